@@ -1,0 +1,192 @@
+/*
+ * miniaero_gpu.h -- C ABI of libminiaero_gpu.so, the GB300 (sm_103a)
+ * implementation of miniAero's explicit RK4 residual path.
+ *
+ * Plain C types only: pointers, sizes, status codes. The library owns all
+ * device memory; host pointers passed in are borrowed for the duration of the
+ * call. Every function returns ma_status (0 = MA_OK); on failure
+ * ma_last_error() returns a message for the calling thread. No C++ exception
+ * crosses this boundary.
+ *
+ * Each entry point names the reference interface it replaces
+ * (kokkos/<file>:<line> in Mantevo miniAero).
+ */
+#ifndef MINIAERO_GPU_H_
+#define MINIAERO_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MA_ABI_VERSION 1
+
+typedef enum {
+  MA_OK = 0,
+  MA_EINVAL = 1,     /* bad argument or option */
+  MA_ENOMEM = 2,     /* host or device allocation failed */
+  MA_ECUDA = 3,      /* CUDA runtime error (no device, launch failure, ...) */
+  MA_EBUDGET = 4,    /* request does not fit the device-memory budget */
+  MA_ETIMEDOUT = 5,  /* bounded wait expired */
+  MA_ENUMERIC = 6,   /* non-finite or non-physical state detected */
+  MA_ESTATE = 7,     /* call not valid in the object's current state */
+  MA_EIO = 8,        /* file could not be read or written */
+  MA_ENOTFOUND = 9   /* unknown id */
+} ma_status;
+
+enum { MA_BC_EXTRAPOLATE = 0, MA_BC_TANGENT = 1, MA_BC_INFLOW = 2, MA_BC_NOSLIP = 3 };
+enum { MA_LIMITER_VENKAT = 0, MA_LIMITER_VANALBADA = 1 };
+enum { MA_VISC_SUTHERLAND = 0, MA_VISC_CONSTANT = 1 };
+enum { MA_PREC_FP64 = 0, MA_PREC_MIXED = 1 };
+/* State layouts: AOS is View<double*[5]> LayoutRight (U[c*5+k], the
+ * reference's host layout); SOA is U[k*ncells+c]. */
+enum { MA_LAYOUT_AOS = 0, MA_LAYOUT_SOA = 1 };
+/* Initial conditions. */
+enum { MA_IC_REFERENCE = 0, MA_IC_SOD = 1, MA_IC_CONSTANT = 2 };
+
+/* Run options: the nine values of miniaero.inp (kokkos/Options.h:47-102)
+ * followed by extension keys the reference hard-codes. */
+typedef struct {
+  int32_t problem_type;       /* 0 Sod, 1 viscous flat plate, 2 inviscid ramp */
+  double lx, ly, lz, angle;
+  int32_t nx, ny, nz;
+  int32_t ntimesteps;
+  double dt;
+  int32_t output_results;
+  int32_t output_frequency;
+  int32_t second_order_space;
+  int32_t viscous;
+  /* extensions (defaults reproduce the reference) */
+  int32_t limiter;            /* MA_LIMITER_*; reference: Venkatakrishnan */
+  int32_t viscosity_model;    /* MA_VISC_*; reference: Sutherland, Pr 0.71 */
+  double mu;                  /* constant viscosity */
+  double prandtl;             /* Prandtl number for the constant model */
+  int32_t precision;          /* MA_PREC_* */
+  double cfl;                 /* > 0: dt = cfl * min_c V_c / sum_f(|u.n| + c|n|) at t = 0 */
+  int32_t ic;                 /* MA_IC_* */
+  double sod_left[2];         /* (rho, p) left of the split (MA_IC_SOD) */
+  double sod_right[2];        /* (rho, p) right of the split */
+  double sod_split;           /* split position in x; <= 0 means lx/2 */
+  int32_t inflow_given;       /* 1: use inflow_state below */
+  double inflow_state[5];     /* conserved inflow / constant state */
+  int32_t bc_override[6];     /* per side (bottom, top, front, back, right, left), -1 = default map */
+  int32_t keep_residual;      /* 1: keep the last stage residual on the device */
+} ma_options;
+
+/* One face list; mirrors Faces<Device> (kokkos/Faces.h:42-71). Vector
+ * fields are [nfaces*3] row-major, conn and flux_index [nfaces*2]. */
+typedef struct {
+  int32_t nfaces;
+  int32_t type;               /* MA_BC_* for boundary sets, -1 for internal */
+  const int32_t* conn;        /* (elem1, elem2); elem2 = -1 on the boundary */
+  const int32_t* flux_index;  /* may be NULL */
+  const double* coords;
+  const double* normal;
+  const double* tangent;
+  const double* binormal;
+  const int32_t* permutation; /* iteration order (Faces::permute_vector_) */
+} ma_face_set;
+
+#define MA_MAX_BC_SETS 16
+
+/* A mesh as the reference's MeshData holds it (kokkos/MeshData.h:42-58). */
+typedef struct {
+  int32_t ncells;
+  const double* cell_coords;  /* [ncells*3] */
+  const double* cell_volumes; /* [ncells] */
+  ma_face_set internal;
+  int32_t nbc;
+  ma_face_set bc[MA_MAX_BC_SETS]; /* boundary_faces order */
+} ma_mesh_view;
+
+typedef struct ma_host_mesh ma_host_mesh;
+typedef struct ma_mesh ma_mesh;
+typedef struct ma_solver ma_solver;
+
+/* ---- library ------------------------------------------------------------ */
+int32_t ma_abi_version(void);
+const char* ma_last_error(void);
+const char* ma_status_string(ma_status s);
+/* Number of CUDA devices visible (0 without a GPU). */
+int32_t ma_device_count(void);
+
+/* ---- options ------------------------------------------------------------ */
+/* Defaults of Options::Options() (kokkos/Options.h:59-69) plus extensions. */
+void ma_options_default(ma_options* o);
+/* Options::read_options_file (kokkos/Options.h:73-101): reads the nine
+ * positional values, then optional "key value" extension lines. Unlike the
+ * reference, a missing file or a malformed value is an error (MA_EIO /
+ * MA_EINVAL), not a silent default. */
+ma_status ma_options_read(const char* path, ma_options* o);
+
+/* ---- host mesh (replaces Parallel3DMesh + MeshProcessor, single rank) ---- */
+/* Parallel3DMesh::Parallel3DMesh + fillMeshData (kokkos/Parallel3DMesh.C:36,
+ * Parallel3DMesh.h:173-449): builds cells, faces, BC sets and the face
+ * iteration permutations on the host. */
+ma_status ma_host_mesh_build(const ma_options* o, ma_host_mesh** out);
+ma_status ma_host_mesh_view(const ma_host_mesh* m, ma_mesh_view* view);
+void ma_host_mesh_free(ma_host_mesh* m);
+/* Initial state on the host (kokkos/Initial_Conditions.h:38-133), U in AOS. */
+ma_status ma_host_initial_state(const ma_host_mesh* m, const ma_options* o, double* U);
+
+/* ---- device mesh (replaces copy_faces / copy_cell_data, Faces.h:88,
+ *      Cells.h:127) --------------------------------------------------------- */
+/* Uploads any mesh given as ma_mesh_view: builds the device face order, the
+ * per-face Roe frame and the per-cell ordered contribution lists that replay
+ * the reference's serial accumulation order. */
+ma_status ma_mesh_upload(const ma_mesh_view* view, ma_mesh** out);
+void ma_mesh_free(ma_mesh* m);
+/* Device bytes held by the mesh. */
+size_t ma_mesh_device_bytes(const ma_mesh* m);
+
+/* ---- solver (replaces TimeSolverExplicitRK4, TimeSolverExplicitRK4.h:164) */
+/* TimeSolverExplicitRK4(MeshData&, const Options&). dt comes from o->dt, or
+ * from o->cfl when > 0 (evaluated on the state given to set_state / init). */
+ma_status ma_solver_create(ma_mesh* mesh, const ma_options* o, ma_solver** out);
+void ma_solver_free(ma_solver* s);
+/* Initial conditions of Solve() (TimeSolverExplicitRK4.h:324-336). */
+ma_status ma_solver_init_state(ma_solver* s, const ma_host_mesh* host_mesh);
+ma_status ma_solver_set_state(ma_solver* s, const double* U, int32_t layout);
+ma_status ma_solver_get_state(ma_solver* s, double* U, int32_t layout);
+/* Residual of the last stage (Solve's res_vec); needs keep_residual. */
+ma_status ma_solver_get_residual(ma_solver* s, double* res, int32_t layout);
+/* nsteps RK4 steps (the body of Solve's time loop, :340-491), asynchronous
+ * on the solver's stream. */
+ma_status ma_solver_step(ma_solver* s, int32_t nsteps);
+ma_status ma_solver_synchronize(ma_solver* s);
+/* The solver's cudaStream_t, for event timing by the caller. */
+void* ma_solver_stream(ma_solver* s);
+double ma_solver_dt(const ma_solver* s);
+int64_t ma_solver_steps_done(const ma_solver* s);
+/* Kernel launches issued per RK4 step (for launch accounting). */
+int32_t ma_solver_launches_per_step(const ma_solver* s);
+/* Sets dt explicitly (after create). */
+ma_status ma_solver_set_dt(ma_solver* s, double dt);
+/* Checks the state for non-finite values or non-positive density/energy;
+ * returns MA_ENUMERIC and the first bad cell in *bad_cell if found. */
+ma_status ma_solver_check_state(ma_solver* s, int64_t* bad_cell);
+/* One full solve as the reference's Solve(): init + ntimesteps steps. */
+ma_status ma_solver_solve(ma_solver* s, const ma_host_mesh* host_mesh);
+
+/* ---- operator-level entry points (unit parity; host arrays in and out) --- */
+/* roe_flux::compute_flux (Roe_Flux.h:50) on n independent faces:
+ * pl, pr [n*5] primitives; normal, tangent, binormal [n*3]; flux [n*5]. */
+ma_status ma_op_roe_flux(int32_t n, const double* pl, const double* pr, const double* normal,
+                         const double* tangent, const double* binormal, double* flux);
+/* newtonian_viscous_flux::compute_flux (Viscous_Flux.h:66): grad [n*15]
+ * (component-major 5x3), prim [n*5], area [n*3], vflux [n*5]. */
+ma_status ma_op_viscous_flux(int32_t n, const double* grad, const double* prim, const double* area,
+                             int32_t viscosity_model, double mu, double prandtl, double* vflux);
+/* VenkatLimiter::limit (VenkatLimiter.h:45) or VanAlbadaLimiter::limit
+ * (VanAlbadaLimiter.h:45), element-wise over n values (d2 ignored by Van Albada). */
+ma_status ma_op_limiter(int32_t n, int32_t kind, const double* dumax, const double* dumin,
+                        const double* du, const double* d2, double* phi);
+/* ComputePrimitives (GasModel.h:69), U and V [n*5]. */
+ma_status ma_op_primitives(int32_t n, const double* U, double* V);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,360 @@
+"""miniaero_gb300: GB300-native miniAero explicit RK4 residual path.
+
+Python host-side mirror of the reference's interface for this path, over the
+C ABI of libminiaero_gpu.so (include/miniaero_gpu.h):
+
+  Options                   kokkos/Options.h:47-102 (miniaero.inp + extensions)
+  Parallel3DMesh            kokkos/Parallel3DMesh.h:56-520 (single rank)
+  MeshData                  kokkos/MeshData.h:42-58 (host copy)
+  TimeSolverExplicitRK4     kokkos/TimeSolverExplicitRK4.h:160-539
+  roe_flux, viscous_flux, venkat_limit, vanalbada_limit, compute_primitives
+                            operator-level entry points (Roe_Flux.h:50,
+                            Viscous_Flux.h:66, VenkatLimiter.h:45,
+                            VanAlbadaLimiter.h:45, GasModel.h:69)
+
+All numerical work runs on the GPU through the library; a missing library or
+GPU raises MiniaeroError instead of falling back to the CPU.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import (MA_BC_EXTRAPOLATE, MA_BC_INFLOW, MA_BC_NOSLIP, MA_BC_TANGENT, MA_IC_CONSTANT,
+                   MA_IC_REFERENCE, MA_IC_SOD, MA_LAYOUT_AOS, MA_LAYOUT_SOA, MA_LIMITER_VANALBADA,
+                   MA_LIMITER_VENKAT, MA_PREC_FP64, MA_PREC_MIXED, MA_VISC_CONSTANT, MA_VISC_SUTHERLAND,
+                   MiniaeroError, check, f64p, i32p, lib)
+
+__all__ = [
+    "Options", "Parallel3DMesh", "MeshData", "FaceSet", "DeviceMesh", "TimeSolverExplicitRK4",
+    "initial_state", "roe_flux", "viscous_flux", "venkat_limit", "vanalbada_limit", "compute_primitives",
+    "device_count", "MiniaeroError", "BC_NAMES",
+    "MA_BC_EXTRAPOLATE", "MA_BC_TANGENT", "MA_BC_INFLOW", "MA_BC_NOSLIP",
+    "MA_LIMITER_VENKAT", "MA_LIMITER_VANALBADA", "MA_VISC_SUTHERLAND", "MA_VISC_CONSTANT",
+    "MA_PREC_FP64", "MA_PREC_MIXED", "MA_IC_REFERENCE", "MA_IC_SOD", "MA_IC_CONSTANT",
+    "MA_LAYOUT_AOS", "MA_LAYOUT_SOA",
+]
+
+BC_NAMES = {MA_BC_EXTRAPOLATE: "Extrapolate", MA_BC_TANGENT: "Tangent", MA_BC_INFLOW: "Inflow",
+            MA_BC_NOSLIP: "NoSlip"}
+
+
+def device_count():
+    return int(lib().ma_device_count())
+
+
+class Options:
+    """Run options: the nine miniaero.inp values plus extension keys."""
+
+    def __init__(self, **kw):
+        object.__setattr__(self, "_o", _lib.ma_options())
+        lib().ma_options_default(ctypes.byref(self._o))
+        for k, v in kw.items():
+            setattr(self, k, v)
+
+    @classmethod
+    def read_options_file(cls, path="miniaero.inp"):
+        """Options::read_options_file; raises on a missing or malformed file."""
+        o = cls()
+        check(lib().ma_options_read(str(path).encode(), ctypes.byref(o._o)))
+        return o
+
+    def __getattr__(self, name):
+        o = object.__getattribute__(self, "_o")
+        v = getattr(o, name)
+        if isinstance(v, ctypes.Array):
+            return list(v)
+        return v
+
+    def __setattr__(self, name, value):
+        o = self._o
+        cur = getattr(o, name)
+        if isinstance(cur, ctypes.Array):
+            if len(value) != len(cur):
+                raise ValueError("%s needs %d values" % (name, len(cur)))
+            for i, x in enumerate(value):
+                cur[i] = x
+        else:
+            setattr(o, name, value)
+
+    def copy(self):
+        c = Options()
+        ctypes.memmove(ctypes.byref(c._o), ctypes.byref(self._o), ctypes.sizeof(self._o))
+        return c
+
+    @property
+    def c(self):
+        return self._o
+
+    def __repr__(self):
+        fields = ", ".join("%s=%r" % (n, getattr(self, n)) for n, _ in _lib.ma_options._fields_)
+        return "Options(%s)" % fields
+
+
+class FaceSet:
+    """Host copy of one Faces<Device> list (kokkos/Faces.h:42-71)."""
+
+    def __init__(self, fs, name):
+        n = fs.nfaces
+        self.name = name
+        self.type = fs.type
+        self.nfaces = n
+
+        def arr(p, shape, dtype):
+            if n == 0:
+                return np.zeros(shape, dtype)
+            return np.ctypeslib.as_array(p, shape=shape).astype(dtype, copy=True)
+
+        self.conn = arr(fs.conn, (n, 2), np.int32)
+        self.coords = arr(fs.coords, (n, 3), np.float64)
+        self.normal = arr(fs.normal, (n, 3), np.float64)
+        self.tangent = arr(fs.tangent, (n, 3), np.float64)
+        self.binormal = arr(fs.binormal, (n, 3), np.float64)
+        self.permutation = arr(fs.permutation, (n,), np.int32)
+
+    def to_c(self):
+        fs = _lib.ma_face_set()
+        fs.nfaces = self.nfaces
+        fs.type = self.type
+        fs.conn = i32p(self.conn)
+        fs.flux_index = ctypes.cast(None, _lib.P_i32)
+        fs.coords = f64p(self.coords)
+        fs.normal = f64p(self.normal)
+        fs.tangent = f64p(self.tangent)
+        fs.binormal = f64p(self.binormal)
+        fs.permutation = i32p(self.permutation)
+        return fs
+
+
+class MeshData:
+    """Mesh as the reference's MeshData holds it, in host numpy arrays."""
+
+    def __init__(self, ncells, cell_coords, cell_volumes, internal, bc, handle=None):
+        self.ncells = ncells
+        self.cell_coords = cell_coords
+        self.cell_volumes = cell_volumes
+        self.internal = internal
+        self.bc = bc
+        self._handle = handle
+
+    def view(self):
+        """ma_mesh_view pointing into this object's arrays (keep self alive)."""
+        v = _lib.ma_mesh_view()
+        v.ncells = self.ncells
+        v.cell_coords = f64p(self.cell_coords)
+        v.cell_volumes = f64p(self.cell_volumes)
+        v.internal = self.internal.to_c()
+        v.nbc = len(self.bc)
+        for i, b in enumerate(self.bc):
+            v.bc[i] = b.to_c()
+        return v
+
+    def __del__(self):
+        h = getattr(self, "_handle", None)
+        if h:
+            try:
+                lib().ma_host_mesh_free(h)
+            except Exception:
+                pass
+            self._handle = None
+
+
+class Parallel3DMesh:
+    """Structured box (or ramp) Hexa8 mesh in unstructured form, one rank."""
+
+    def __init__(self, nx, ny, nz, lx, ly, lz, problem_type, angle=0.0, bc_override=None):
+        self.options = Options(nx=nx, ny=ny, nz=nz, lx=lx, ly=ly, lz=lz, problem_type=problem_type, angle=angle)
+        if bc_override is not None:
+            self.options.bc_override = bc_override
+
+    @classmethod
+    def from_options(cls, options):
+        m = cls.__new__(cls)
+        m.options = options.copy()
+        return m
+
+    def fill_mesh_data(self):
+        L = lib()
+        h = ctypes.c_void_p()
+        check(L.ma_host_mesh_build(ctypes.byref(self.options.c), ctypes.byref(h)))
+        v = _lib.ma_mesh_view()
+        check(L.ma_host_mesh_view(h, ctypes.byref(v)))
+        C = v.ncells
+        coords = np.ctypeslib.as_array(v.cell_coords, shape=(C, 3)).copy()
+        vols = np.ctypeslib.as_array(v.cell_volumes, shape=(C,)).copy()
+        internal = FaceSet(v.internal, "internal")
+        bc = [FaceSet(v.bc[i], BC_NAMES[v.bc[i].type]) for i in range(v.nbc)]
+        return MeshData(C, coords, vols, internal, bc, handle=h)
+
+
+def initial_state(mesh_data, options):
+    """Initial conserved state (kokkos/Initial_Conditions.h), shape (ncells, 5)."""
+    if mesh_data._handle is None:
+        raise ValueError("initial_state needs a MeshData built by Parallel3DMesh")
+    U = np.empty((mesh_data.ncells, 5), np.float64)
+    check(lib().ma_host_initial_state(mesh_data._handle, ctypes.byref(options.c), f64p(U)))
+    return U
+
+
+class DeviceMesh:
+    """Device copy of a MeshData (ma_mesh_upload); shareable by solvers."""
+
+    def __init__(self, mesh_data):
+        self._mesh_data = mesh_data
+        self._view = mesh_data.view()
+        self._h = ctypes.c_void_p()
+        check(lib().ma_mesh_upload(ctypes.byref(self._view), ctypes.byref(self._h)))
+        self.ncells = mesh_data.ncells
+
+    @property
+    def device_bytes(self):
+        return int(lib().ma_mesh_device_bytes(self._h))
+
+    def close(self):
+        if self._h:
+            lib().ma_mesh_free(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class TimeSolverExplicitRK4:
+    """RK4 solver on the GPU (kokkos/TimeSolverExplicitRK4.h:160-539)."""
+
+    def __init__(self, mesh_data, options, device_mesh=None):
+        self.options = options.copy()
+        self.mesh_data = mesh_data
+        self.device_mesh = device_mesh if device_mesh is not None else DeviceMesh(mesh_data)
+        self._h = ctypes.c_void_p()
+        check(lib().ma_solver_create(self.device_mesh._h, ctypes.byref(self.options.c), ctypes.byref(self._h)))
+        self.ncells = mesh_data.ncells
+
+    # -- state ---------------------------------------------------------------
+    def set_state(self, U):
+        U = np.ascontiguousarray(U, dtype=np.float64).reshape(self.ncells, 5)
+        check(lib().ma_solver_set_state(self._h, f64p(U), MA_LAYOUT_AOS))
+
+    def init_state(self):
+        check(lib().ma_solver_init_state(self._h, self.mesh_data._handle))
+
+    def get_state(self):
+        U = np.empty((self.ncells, 5), np.float64)
+        check(lib().ma_solver_get_state(self._h, f64p(U), MA_LAYOUT_AOS))
+        return U
+
+    def get_residual(self):
+        R = np.empty((self.ncells, 5), np.float64)
+        check(lib().ma_solver_get_residual(self._h, f64p(R), MA_LAYOUT_AOS))
+        return R
+
+    # -- time stepping ---------------------------------------------------------
+    def step(self, nsteps=1):
+        check(lib().ma_solver_step(self._h, int(nsteps)))
+
+    def synchronize(self):
+        check(lib().ma_solver_synchronize(self._h))
+
+    def solve(self):
+        """Solve(): initial state then options.ntimesteps steps; returns U."""
+        self.init_state()
+        self.step(self.options.ntimesteps)
+        self.synchronize()
+        return self.get_state()
+
+    def check_state(self):
+        bad = ctypes.c_int64(-1)
+        st = lib().ma_solver_check_state(self._h, ctypes.byref(bad))
+        return st, bad.value
+
+    @property
+    def dt(self):
+        return float(lib().ma_solver_dt(self._h))
+
+    @dt.setter
+    def dt(self, value):
+        check(lib().ma_solver_set_dt(self._h, float(value)))
+
+    @property
+    def stream(self):
+        return lib().ma_solver_stream(self._h)
+
+    @property
+    def steps_done(self):
+        return int(lib().ma_solver_steps_done(self._h))
+
+    @property
+    def launches_per_step(self):
+        return int(lib().ma_solver_launches_per_step(self._h))
+
+    def close(self):
+        if self._h:
+            lib().ma_solver_free(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+# ---- operator-level entry points -------------------------------------------------
+def _a(x, shape):
+    return np.ascontiguousarray(x, dtype=np.float64).reshape(shape)
+
+
+def roe_flux(pl, pr, normal, tangent, binormal):
+    """roe_flux::compute_flux on n faces; primitives (n,5), vectors (n,3)."""
+    pl = _a(pl, (-1, 5))
+    n = pl.shape[0]
+    pr, nm, tg, bn = _a(pr, (n, 5)), _a(normal, (n, 3)), _a(tangent, (n, 3)), _a(binormal, (n, 3))
+    out = np.empty((n, 5), np.float64)
+    check(lib().ma_op_roe_flux(n, f64p(pl), f64p(pr), f64p(nm), f64p(tg), f64p(bn), f64p(out)))
+    return out
+
+
+def viscous_flux(grad, prim, area, viscosity_model=MA_VISC_SUTHERLAND, mu=0.0, prandtl=0.72):
+    """newtonian_viscous_flux::compute_flux; grad (n,5,3), prim (n,5), area (n,3)."""
+    grad = _a(grad, (-1, 5, 3))
+    n = grad.shape[0]
+    prim, area = _a(prim, (n, 5)), _a(area, (n, 3))
+    out = np.empty((n, 5), np.float64)
+    check(lib().ma_op_viscous_flux(n, f64p(grad), f64p(prim), f64p(area), viscosity_model, mu, prandtl,
+                                   f64p(out)))
+    return out
+
+
+def venkat_limit(dumax, dumin, du, d2):
+    dumax = _a(dumax, (-1,))
+    n = dumax.shape[0]
+    dumin, du, d2 = _a(dumin, (n,)), _a(du, (n,)), _a(d2, (n,))
+    out = np.empty(n, np.float64)
+    check(lib().ma_op_limiter(n, MA_LIMITER_VENKAT, f64p(dumax), f64p(dumin), f64p(du), f64p(d2), f64p(out)))
+    return out
+
+
+def vanalbada_limit(dumax, dumin, du):
+    dumax = _a(dumax, (-1,))
+    n = dumax.shape[0]
+    dumin, du = _a(dumin, (n,)), _a(du, (n,))
+    out = np.empty(n, np.float64)
+    check(lib().ma_op_limiter(n, MA_LIMITER_VANALBADA, f64p(dumax), f64p(dumin), f64p(du),
+                              ctypes.cast(None, _lib.P_f64), f64p(out)))
+    return out
+
+
+def compute_primitives(U):
+    U = _a(U, (-1, 5))
+    out = np.empty_like(U)
+    check(lib().ma_op_primitives(U.shape[0], f64p(U), f64p(out)))
+    return out

@@ -1,0 +1,103 @@
+// Kernel interface of the RK4 residual path (device views and launchers).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "physics.cuh"
+
+namespace miniaero {
+namespace dev {
+
+constexpr int kMaxCellFaces = 6;  // Hexa8: every face is internal or boundary
+
+// Topology shared by both precisions. Face arrays are in device order:
+// internal faces [0, Fi) sorted by (left, right) cell, then boundary faces
+// [Fi, F) grouped by BC type (Extrapolate, Tangent, NoSlip, Inflow).
+struct TopoView {
+  int32_t C = 0, Fi = 0, Fb = 0, F = 0;
+  int32_t nbc_type[4] = {0, 0, 0, 0};  // BC face counts in type order E, T, N, I
+  const double* vol = nullptr;         // [C]
+  const int32_t* fconn = nullptr;      // [2][F] (left, right); right = -1 on a boundary
+  // Per-cell contribution lists, slot-major [kMaxCellFaces][C], code =
+  // (face << 1) | (cell is the face's left cell), -1 for an unused slot.
+  const int32_t* csr_grad = nullptr;   // Green-Gauss / min-max / limiter order
+  const int32_t* csr_nbr = nullptr;    // neighbour cell of each csr_grad slot (-1 boundary)
+  const int32_t* csr_flux = nullptr;   // residual order
+};
+
+// Geometry in the arithmetic type R of the flux/gradient/limiter work.
+template <class R>
+struct GeomView {
+  const R* vol = nullptr;  // [C]
+  const R* fn = nullptr;   // [3][F] area vector
+  const R* fnu = nullptr;  // [3][F] unit normal
+  const R* ftu = nullptr;  // [3][F] unit tangent
+  const R* fbu = nullptr;  // [3][F] unit binormal
+  const R* fnn = nullptr;  // [F] |n|
+  const R* dL = nullptr;   // [3][F] face centroid - left cell centroid
+  const R* dR = nullptr;   // [3][F] face centroid - right cell centroid (internal faces)
+};
+
+// Per-stage work arrays in type R (SoA, component-major).
+template <class R>
+struct StageBuffers {
+  R* W = nullptr;      // [5][C] primitives of the stage state
+  R* grad = nullptr;   // [15][C] Green-Gauss gradients, (component, direction)
+  R* phi = nullptr;    // [5][C] limiter
+  R* fflux = nullptr;  // [F][5] face flux (internal) or cell contribution (boundary)
+};
+
+struct StateBuffers {
+  double* Un = nullptr;    // [5][C]
+  double* Unp1 = nullptr;  // [5][C]
+  double* res = nullptr;   // [5][C] optional
+};
+
+struct PathConfig {
+  bool second_order = false;
+  bool viscous = false;
+  int limiter = 0;  // 0 Venkatakrishnan, 1 Van Albada
+  Transport transport{0, 0.0, 0.0};
+  double inflow[5] = {0, 0, 0, 0, 0};
+  double dt = 0.0;
+};
+
+// Launch counts per RK stage for the given configuration.
+int launches_per_stage(const PathConfig& cfg, const TopoView& t);
+
+template <class R>
+cudaError_t launch_init_primitives(const TopoView& t, const StateBuffers& s, const StageBuffers<R>& b,
+                                   cudaStream_t stream);
+
+template <class R>
+cudaError_t launch_stage(const TopoView& t, const GeomView<R>& g, const PathConfig& cfg, const StateBuffers& s,
+                         const StageBuffers<R>& b, int stage, cudaStream_t stream);
+
+// Defined in kernels_fp64.cu (plain form) and kernels_mixed.cu (mixed form).
+template <>
+cudaError_t launch_init_primitives<double>(const TopoView&, const StateBuffers&, const StageBuffers<double>&,
+                                           cudaStream_t);
+template <>
+cudaError_t launch_init_primitives<float>(const TopoView&, const StateBuffers&, const StageBuffers<float>&,
+                                          cudaStream_t);
+template <>
+cudaError_t launch_stage<double>(const TopoView&, const GeomView<double>&, const PathConfig&, const StateBuffers&,
+                                 const StageBuffers<double>&, int, cudaStream_t);
+template <>
+cudaError_t launch_stage<float>(const TopoView&, const GeomView<float>&, const PathConfig&, const StateBuffers&,
+                                const StageBuffers<float>&, int, cudaStream_t);
+
+// Operator-level kernels (unit parity, FP64).
+cudaError_t launch_op_roe(int n, const double* pl, const double* pr, const double* normal, const double* tangent,
+                          const double* binormal, double* flux, cudaStream_t stream);
+cudaError_t launch_op_viscous(int n, const double* grad, const double* prim, const double* area, Transport tr,
+                              double* vflux, cudaStream_t stream);
+cudaError_t launch_op_limiter(int n, int kind, const double* dumax, const double* dumin, const double* du,
+                              const double* d2, double* phi, cudaStream_t stream);
+cudaError_t launch_op_primitives(int n, const double* U, double* V, cudaStream_t stream);
+
+// State check: first cell with a non-finite value or non-positive rho / rhoE.
+cudaError_t launch_check_state(int C, const double* Un, unsigned long long* first_bad, cudaStream_t stream);
+
+}  // namespace dev
+}  // namespace miniaero

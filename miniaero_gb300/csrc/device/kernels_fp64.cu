@@ -1,0 +1,22 @@
+// Plain FP64 form. Compiled with --fmad=false: every multiply and add rounds
+// separately, as in the reference's serial build with -ffp-contract=off.
+#include "kernels_impl.cuh"
+
+namespace miniaero {
+namespace dev {
+
+template <>
+cudaError_t launch_init_primitives<double>(const TopoView& t, const StateBuffers& s, const StageBuffers<double>& b,
+                                           cudaStream_t stream) {
+  return launch_init_primitives_impl<double>(t, s, b, stream);
+}
+
+template <>
+cudaError_t launch_stage<double>(const TopoView& t, const GeomView<double>& g, const PathConfig& cfg,
+                                 const StateBuffers& s, const StageBuffers<double>& b, int stage,
+                                 cudaStream_t stream) {
+  return launch_stage_impl<double>(t, g, cfg, s, b, stage, stream);
+}
+
+}  // namespace dev
+}  // namespace miniaero

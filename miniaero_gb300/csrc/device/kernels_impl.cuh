@@ -1,0 +1,379 @@
+// Kernel templates of the RK4 residual path, included by the translation
+// unit of each precision (kernels_fp64.cu with --fmad=false for the plain,
+// bit-exact form; kernels_mixed.cu for the mixed form). Per RK stage:
+//   k_sweep1        cell-centric: Green-Gauss gradient, stencil min/max and
+//                   limiter of one cell from its ordered face list
+//                   (GreenGauss.h:51-270, StencilLimiter.h:56-500)
+//   k_internal_flux face-centric: extrapolation, Roe and viscous flux of one
+//                   internal face (Flux.h:89-180)
+//   k_bc_flux       face-centric: boundary ghost state and flux
+//                   (Extrapolate_BC.h, Tangent_BC.h, NoSlip_BC.h, Inflow_BC.h)
+//   k_residual      cell-centric: ordered face-flux gather, dt/V scaling, RK4
+//                   accumulation and the next stage's primitives
+//                   (Flux.h:188-229, TimeSolverExplicitRK4.h:106-128,352-489)
+// Each accumulator is summed in the reference's serial order (the per-cell
+// lists are built on the host), so the FP64 instantiation reproduces the
+// reference's Serial results bit for bit.
+#pragma once
+#include <cfloat>
+#include <cstdint>
+
+#include "kernels.cuh"
+
+namespace miniaero {
+namespace dev {
+
+namespace {
+
+constexpr int kCellBlock = 256;
+constexpr int kFaceBlock = 128;
+
+// Conserved inflow state passed by value to the boundary kernel.
+struct InflowState {
+  double u[5];
+};
+
+template <class R> __device__ __forceinline__ R big_value();
+template <> __device__ __forceinline__ double big_value<double>() { return 1.0e300; }
+template <> __device__ __forceinline__ float big_value<float>() { return FLT_MAX; }
+
+template <class R>
+__device__ __forceinline__ FaceFrame<R> load_frame(const GeomView<R>& g, int f, int F) {
+  FaceFrame<R> fr;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    fr.n[d] = g.fn[d * F + f];
+    fr.nu[d] = g.fnu[d * F + f];
+    fr.tu[d] = g.ftu[d * F + f];
+    fr.bu[d] = g.fbu[d * F + f];
+  }
+  fr.nn = g.fnn[f];
+  return fr;
+}
+
+// MODE: 0 gradient only (viscous first order), 1 + Venkatakrishnan, 2 + Van Albada.
+template <class R, int MODE>
+__global__ void __launch_bounds__(kCellBlock) k_sweep1(TopoView t, GeomView<R> g, const R* __restrict__ W,
+                                                       R* __restrict__ grad, R* __restrict__ phi) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= t.C) return;
+  const int C = t.C, F = t.F;
+  R wc[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) wc[k] = W[k * C + c];
+  const R V = g.vol[c];
+  R acc[5][3];
+  R mn[5], mx[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) acc[k][d] = R(0.0);
+    mn[k] = big_value<R>();
+    mx[k] = -big_value<R>();
+  }
+  // Gradient contributions and min/max, in the reference's serial face order.
+#pragma unroll 1
+  for (int s = 0; s < kMaxCellFaces; ++s) {
+    const int code = t.csr_grad[s * C + c];
+    if (code < 0) continue;
+    const int f = code >> 1;
+    const bool left = code & 1;
+    const R n[3] = {g.fn[f], g.fn[F + f], g.fn[2 * F + f]};
+    if (f < t.Fi) {
+      const int nb = t.csr_nbr[s * C + c];
+      R wn[5];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) wn[k] = W[k * C + nb];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        const R pl = left ? wc[k] : wn[k];
+        const R pr = left ? wn[k] : wc[k];
+        const R h = R(0.5) * (pl + pr);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const R gr = h * n[d];
+          acc[k][d] += left ? gr / V : -gr / V;
+        }
+        if (MODE > 0) {
+          const R fmin_ = (pr < pl) ? pr : pl;
+          const R fmax_ = (pr > pl) ? pr : pl;
+          mn[k] = (fmin_ < mn[k]) ? fmin_ : mn[k];
+          mx[k] = (mx[k] < fmax_) ? fmax_ : mx[k];
+        }
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) acc[k][d] += wc[k] * n[d] / V;
+        if (MODE > 0) {
+          mn[k] = (wc[k] < mn[k]) ? wc[k] : mn[k];
+          mx[k] = (mx[k] < wc[k]) ? wc[k] : mx[k];
+        }
+      }
+    }
+  }
+  R gsum[5][3];
+#pragma unroll
+  for (int k = 0; k < 5; ++k)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      gsum[k][d] = R(0) + acc[k][d];  // green_gauss_gradient_sum
+      grad[(3 * k + d) * C + c] = gsum[k][d];
+    }
+  if constexpr (MODE > 0) {
+    // Limiter: minimum over this cell's faces of the limiter function.
+    R lim[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) lim[k] = R(1.0);
+#pragma unroll 1
+    for (int s = 0; s < kMaxCellFaces; ++s) {
+      const int code = t.csr_grad[s * C + c];
+      if (code < 0) continue;
+      const int f = code >> 1;
+      const R* dv = (code & 1) ? g.dL : g.dR;
+      const R disp[3] = {dv[f], dv[F + f], dv[2 * F + f]};
+      R dist = 0;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) dist += disp[d] * disp[d];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        R du = 0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) du += disp[d] * gsum[k][d];
+        const R dumax = mx[k] - wc[k];
+        const R dumin = mn[k] - wc[k];
+        const R p = (MODE == 1) ? venkat<R>(dumax, dumin, du, dist) : vanalbada<R>(dumax, dumin, du);
+        lim[k] = (p < lim[k]) ? p : lim[k];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 5; ++k) phi[k * C + c] = lim[k];
+  }
+}
+
+template <class R, bool SECOND, bool VISC>
+__global__ void __launch_bounds__(kFaceBlock) k_internal_flux(TopoView t, GeomView<R> g, const R* __restrict__ W,
+                                                              const R* __restrict__ grad, const R* __restrict__ phi,
+                                                              Transport tr, R* __restrict__ fflux) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= t.Fi) return;
+  const int C = t.C, F = t.F;
+  const int L = t.fconn[f];
+  const int Rc = t.fconn[F + f];
+  R pl[5], pr[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    pl[k] = W[k * C + L];
+    pr[k] = W[k * C + Rc];
+  }
+  if (SECOND) {
+    const R dl[3] = {g.dL[f], g.dL[F + f], g.dL[2 * F + f]};
+    const R dr[3] = {g.dR[f], g.dR[F + f], g.dR[2 * F + f]};
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      R tl = 0, trr = 0;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        tl += dl[d] * grad[(3 * k + d) * C + L];
+        trr += dr[d] * grad[(3 * k + d) * C + Rc];
+      }
+      pl[k] += tl * phi[k * C + L];
+      pr[k] += trr * phi[k * C + Rc];
+    }
+  }
+  const FaceFrame<R> fr = load_frame<R>(g, f, F);
+  R flux[5];
+  roe_flux<R>(pl, pr, fr, flux);
+  if (VISC) {
+    R pf[5], gf[5][3], vf[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      pf[k] = R(0.5) * (pl[k] + pr[k]);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) gf[k][d] = R(0.5) * (grad[(3 * k + d) * C + L] + grad[(3 * k + d) * C + Rc]);
+    }
+    viscous_flux<R>(gf, pf, fr.n, tr, vf);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) flux[k] -= vf[k];
+  }
+#pragma unroll
+  for (int k = 0; k < 5; ++k) fflux[static_cast<size_t>(f) * 5 + k] = flux[k];
+}
+
+// Boundary faces; each writes the contribution its cell adds to the residual.
+template <class R>
+__global__ void __launch_bounds__(kFaceBlock) k_bc_flux(TopoView t, GeomView<R> g, const R* __restrict__ W,
+                                                        Transport tr, InflowState inflow,
+                                                        R* __restrict__ fflux) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= t.Fb) return;
+  const int C = t.C, F = t.F;
+  const int f = t.Fi + i;
+  const int c = t.fconn[f];
+  const int e0 = t.nbc_type[0], e1 = e0 + t.nbc_type[1], e2 = e1 + t.nbc_type[2];
+  R pl[5], pr[5], flux[5], out[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) pl[k] = W[k * C + c];
+  const FaceFrame<R> fr = load_frame<R>(g, f, F);
+  if (i < e0) {  // Extrapolate_BC.h:70-100
+    roe_flux<R>(pl, pl, fr, flux);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) out[k] = -flux[k];
+  } else if (i < e1) {  // Tangent_BC.h:72-121
+    reflect_state<R>(fr.n, fr.nn, pl, pr);
+    roe_flux<R>(pl, pr, fr, flux);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) out[k] = -flux[k];
+  } else if (i < e2) {  // NoSlip_BC.h:77-155
+    reflect_state<R>(fr.n, fr.nn, pl, pr);
+    roe_flux<R>(pl, pr, fr, flux);
+    R pf[5], gf[5][3], vf[5];
+    pf[0] = pl[0]; pf[1] = R(0.0); pf[2] = R(0.0); pf[3] = R(0.0); pf[4] = pl[4];
+    R dist = 0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const R dx = g.dL[d * F + f];
+      dist += dx * dx;
+    }
+    const R inv_d = R(1.0) / dsqrt<R>(dist);
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) gf[k][d] = (pf[k] - pl[k]) * fr.nu[d] * inv_d;
+    viscous_flux<R>(gf, pf, fr.n, tr, vf);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) out[k] = -flux[k] + vf[k];
+  } else {  // Inflow_BC.h:73-109
+    double vi[5];
+    primitives(inflow.u, vi);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) pr[k] = R(vi[k]);
+    roe_flux<R>(pl, pr, fr, flux);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) out[k] = -flux[k];
+  }
+#pragma unroll
+  for (int k = 0; k < 5; ++k) fflux[static_cast<size_t>(f) * 5 + k] = out[k];
+}
+
+// Ordered residual gather + RK4 update + primitives of the next stage state.
+template <class R>
+__global__ void __launch_bounds__(kCellBlock) k_residual(TopoView t, const R* __restrict__ fflux,
+                                                         double* __restrict__ Un, double* __restrict__ Unp1,
+                                                         R* __restrict__ W, double* __restrict__ res_out, double dt,
+                                                         int stage) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= t.C) return;
+  const int C = t.C;
+  double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+#pragma unroll 1
+  for (int s = 0; s < kMaxCellFaces; ++s) {
+    const int code = t.csr_flux[s * C + c];
+    if (code < 0) continue;
+    const int f = code >> 1;
+    const bool neg = (code & 1) && f < t.Fi;
+    const R* fp = fflux + static_cast<size_t>(f) * 5;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      const double v = static_cast<double>(fp[k]);
+      acc[k] += neg ? -v : v;
+    }
+  }
+  // RK4 coefficients (TimeSolverExplicitRK4.h:188-195): beta of this stage and
+  // alpha of the stage that follows (alpha[0] = 0 after the last stage).
+  double beta, alpha_next;
+  switch (stage) {
+    case 0: beta = 1.0 / 6.0; alpha_next = 1.0 / 2.0; break;
+    case 1: beta = 1.0 / 3.0; alpha_next = 1.0 / 2.0; break;
+    case 2: beta = 1.0 / 3.0; alpha_next = 1.0; break;
+    default: beta = 1.0 / 6.0; alpha_next = 0.0; break;
+  }
+  const double dtv = dt / t.vol[c];
+  double ut[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const double r = 0.0 + dtv * acc[k];
+    if (res_out) res_out[k * C + c] = r;
+    if (stage == 0) {
+      const double un = Un[k * C + c];
+      Unp1[k * C + c] = un + beta * r;
+      ut[k] = un + alpha_next * r;
+    } else if (stage < 3) {
+      const double un = Un[k * C + c];
+      Unp1[k * C + c] = Unp1[k * C + c] + beta * r;
+      ut[k] = un + alpha_next * r;
+    } else {
+      const double u1 = Unp1[k * C + c] + beta * r;
+      Un[k * C + c] = u1;
+      ut[k] = u1 + alpha_next * r;
+    }
+  }
+  double v[5];
+  primitives(ut, v);
+#pragma unroll
+  for (int k = 0; k < 5; ++k) W[k * C + c] = static_cast<R>(v[k]);
+}
+
+// Primitives of U_n + 0 * res with res = 0 (first stage after set_state).
+template <class R>
+__global__ void k_init_primitives(int C, const double* __restrict__ Un, R* __restrict__ W, double zero) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  double ut[5], v[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) ut[k] = Un[k * C + c] + 0.0 * zero;
+  primitives(ut, v);
+#pragma unroll
+  for (int k = 0; k < 5; ++k) W[k * C + c] = static_cast<R>(v[k]);
+}
+
+inline unsigned blocks_for(int n, int bs) { return static_cast<unsigned>((n + bs - 1) / bs); }
+
+template <class R>
+cudaError_t launch_init_primitives_impl(const TopoView& t, const StateBuffers& s, const StageBuffers<R>& b,
+                                        cudaStream_t stream) {
+  if (t.C == 0) return cudaSuccess;
+  k_init_primitives<R><<<blocks_for(t.C, kCellBlock), kCellBlock, 0, stream>>>(t.C, s.Un, b.W, 0.0);
+  return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t launch_stage_impl(const TopoView& t, const GeomView<R>& g, const PathConfig& cfg, const StateBuffers& s,
+                              const StageBuffers<R>& b, int stage, cudaStream_t stream) {
+  if (t.C == 0) return cudaSuccess;
+  const unsigned gc = blocks_for(t.C, kCellBlock);
+  if (cfg.second_order) {
+    if (cfg.limiter == 1)
+      k_sweep1<R, 2><<<gc, kCellBlock, 0, stream>>>(t, g, b.W, b.grad, b.phi);
+    else
+      k_sweep1<R, 1><<<gc, kCellBlock, 0, stream>>>(t, g, b.W, b.grad, b.phi);
+  } else if (cfg.viscous) {
+    k_sweep1<R, 0><<<gc, kCellBlock, 0, stream>>>(t, g, b.W, b.grad, b.phi);
+  }
+  if (t.Fi > 0) {
+    const unsigned gf = blocks_for(t.Fi, kFaceBlock);
+    if (cfg.second_order) {
+      if (cfg.viscous)
+        k_internal_flux<R, true, true><<<gf, kFaceBlock, 0, stream>>>(t, g, b.W, b.grad, b.phi, cfg.transport, b.fflux);
+      else
+        k_internal_flux<R, true, false><<<gf, kFaceBlock, 0, stream>>>(t, g, b.W, b.grad, b.phi, cfg.transport, b.fflux);
+    } else {
+      if (cfg.viscous)
+        k_internal_flux<R, false, true><<<gf, kFaceBlock, 0, stream>>>(t, g, b.W, b.grad, b.phi, cfg.transport, b.fflux);
+      else
+        k_internal_flux<R, false, false><<<gf, kFaceBlock, 0, stream>>>(t, g, b.W, b.grad, b.phi, cfg.transport, b.fflux);
+    }
+  }
+  if (t.Fb > 0) {
+    InflowState inflow;
+    for (int k = 0; k < 5; ++k) inflow.u[k] = cfg.inflow[k];
+    k_bc_flux<R><<<blocks_for(t.Fb, kFaceBlock), kFaceBlock, 0, stream>>>(t, g, b.W, cfg.transport, inflow, b.fflux);
+  }
+  k_residual<R><<<gc, kCellBlock, 0, stream>>>(t, b.fflux, s.Un, s.Unp1, b.W, s.res, cfg.dt, stage);
+  return cudaGetLastError();
+}
+
+}  // namespace
+}  // namespace dev
+}  // namespace miniaero

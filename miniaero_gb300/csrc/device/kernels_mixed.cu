@@ -1,0 +1,22 @@
+// Mixed form: FP32 face flux, gradient and limiter; FP64 residual
+// accumulation, RK4 update and primitives of the FP64 state.
+#include "kernels_impl.cuh"
+
+namespace miniaero {
+namespace dev {
+
+template <>
+cudaError_t launch_init_primitives<float>(const TopoView& t, const StateBuffers& s, const StageBuffers<float>& b,
+                                          cudaStream_t stream) {
+  return launch_init_primitives_impl<float>(t, s, b, stream);
+}
+
+template <>
+cudaError_t launch_stage<float>(const TopoView& t, const GeomView<float>& g, const PathConfig& cfg,
+                                const StateBuffers& s, const StageBuffers<float>& b, int stage,
+                                cudaStream_t stream) {
+  return launch_stage_impl<float>(t, g, cfg, s, b, stage, stream);
+}
+
+}  // namespace dev
+}  // namespace miniaero

@@ -1,0 +1,245 @@
+// Device physics for the RK4 residual path.
+//
+// Every function is templated on the arithmetic type R of the flux, gradient
+// and limiter work: R = double is the plain form and keeps, expression by
+// expression, the operand order of the reference functors so that (built with
+// --fmad=false) results are bit-identical to the reference's serial run;
+// R = float is the mixed form's fast path.
+//
+//   primitives           kokkos/GasModel.h:69-90
+//   roe_flux             kokkos/Roe_Flux.h:50-265
+//   viscous_flux         kokkos/Viscous_Flux.h:66-98, GasModel.h:92-106
+//   venkat / vanalbada   kokkos/VenkatLimiter.h:45-73, VanAlbadaLimiter.h:45-65
+//   reflect_state        kokkos/Tangent_BC.h:86-102, NoSlip_BC.h:93-109
+#pragma once
+#include <cuda_runtime.h>
+#include <cfloat>
+
+namespace miniaero {
+namespace dev {
+
+template <class R> __device__ __forceinline__ R dsqrt(R x);
+template <> __device__ __forceinline__ double dsqrt<double>(double x) { return sqrt(x); }
+template <> __device__ __forceinline__ float dsqrt<float>(float x) { return sqrtf(x); }
+template <class R> __device__ __forceinline__ R dabs(R x);
+template <> __device__ __forceinline__ double dabs<double>(double x) { return fabs(x); }
+template <> __device__ __forceinline__ float dabs<float>(float x) { return fabsf(x); }
+
+// Conserved -> primitive (rho, u, v, w, T); always FP64 (the state is FP64).
+__device__ __forceinline__ void primitives(const double U[5], double V[5]) {
+  const double gamma = 1.4;
+  const double Rgas = 287.05;
+  const double r = U[0];
+  const double ri = 1.0 / r;
+  const double u = U[1] * ri;
+  const double v = U[2] * ri;
+  const double w = U[3] * ri;
+  const double k = 0.5 * (u * u + v * v + w * w);
+  const double e = U[4] * ri - k;
+  const double T = e * (gamma - 1.0) / Rgas;
+  V[0] = r; V[1] = u; V[2] = v; V[3] = w; V[4] = T;
+}
+
+// Face frame precomputed once per mesh from the reference's own expressions:
+// |n| = sqrt(n.n) and the three unit vectors n/|n|, t/|t|, b/|b|.
+template <class R>
+struct FaceFrame {
+  R n[3];    // area vector
+  R nu[3];   // unit normal
+  R tu[3];   // unit tangent
+  R bu[3];   // unit binormal
+  R nn;      // |n|
+};
+
+// Roe approximate Riemann flux on primitive states.
+template <class R>
+__device__ __forceinline__ void roe_flux(const R pl[5], const R pr[5], const FaceFrame<R>& f, R flux[5]) {
+  const R efix_u = R(0.1), efix_c = R(0.1), gm1 = R(0.4);
+  const R* n = f.n;
+  const R rl = pl[0], ul = pl[1], vl = pl[2], wl = pl[3];
+  const R p_l = rl * R(287.05) * pl[4];
+  const R h_l = R(1004.0) * pl[4];
+  const R H_l = h_l + R(0.5) * (ul * ul + vl * vl + wl * wl);
+  const R mf_l = rl * (n[0] * ul + n[1] * vl + n[2] * wl);
+  const R rr = pr[0], ur = pr[1], vr = pr[2], wr = pr[3];
+  const R p_r = rr * R(287.05) * pr[4];
+  const R h_r = R(1004.0) * pr[4];
+  const R H_r = h_r + R(0.5) * (ur * ur + vr * vr + wr * wr);
+  const R mf_r = rr * (n[0] * ur + n[1] * vr + n[2] * wr);
+  const R psum = p_l + p_r;
+
+  flux[0] = R(0.5) * (mf_l + mf_r);
+  flux[1] = R(0.5) * (mf_l * ul + mf_r * ur + n[0] * psum);
+  flux[2] = R(0.5) * (mf_l * vl + mf_r * vr + n[1] * psum);
+  flux[3] = R(0.5) * (mf_l * wl + mf_r * wr + n[2] * psum);
+  flux[4] = R(0.5) * (mf_l * H_l + mf_r * H_r);
+
+  const R* nu = f.nu;
+  const R* tu = f.tu;
+  const R* bu = f.bu;
+  const R srl = dsqrt<R>(rl);
+  const R denom = R(1.0) / (srl + dsqrt<R>(rr));
+  const R alpha = srl * denom;
+  const R beta = R(1.0) - alpha;
+  const R uroe = alpha * ul + beta * ur;
+  const R vroe = alpha * vl + beta * vr;
+  const R wroe = alpha * wl + beta * wr;
+  const R hroe = alpha * h_l + beta * h_r +
+                 R(0.5) * alpha * beta *
+                     ((ur - ul) * (ur - ul) + (vr - vl) * (vr - vl) + (wr - wl) * (wr - wl));
+  const R c = dsqrt<R>(gm1 * hroe);
+
+  const R nv = uroe * nu[0] + vroe * nu[1] + wroe * nu[2];
+  const R tv = uroe * tu[0] + vroe * tu[1] + wroe * tu[2];
+  const R bv = uroe * bu[0] + vroe * bu[1] + wroe * bu[2];
+  const R ke = R(0.5) * (uroe * uroe + vroe * vroe + wroe * wroe);
+  const R cssi = R(1.0) / (c * c);
+  const R hcssi = R(0.5) * cssi;
+
+  R dq[5];
+  dq[0] = rr - rl;
+  dq[1] = rr * ur - rl * ul;
+  dq[2] = rr * vr - rl * vl;
+  dq[3] = rr * wr - rl * wl;
+  dq[4] = (rr * H_r - p_r) - (rl * H_l - p_l);
+
+  const R cbar = c * f.nn;
+  const R ubar = uroe * n[0] + vroe * n[1] + wroe * n[2];
+  const R cfl = dabs<R>(ubar) + cbar;
+  const R eig1 = ubar + cbar, eig2 = ubar - cbar, eig3 = ubar;
+  R a1 = dabs<R>(eig1), a2 = dabs<R>(eig2), a3 = dabs<R>(eig3);
+  const R epuc = efix_u * cfl, epcc = efix_c * cfl;
+  if (a1 < epcc) a1 = R(0.5) * (eig1 * eig1 + epcc * epcc) / epcc;
+  if (a2 < epcc) a2 = R(0.5) * (eig2 * eig2 + epcc * epcc) / epcc;
+  if (a3 < epuc) a3 = R(0.5) * (eig3 * eig3 + epuc * epuc) / epuc;
+  // |lambda| per characteristic: eigp - eigm of the reference.
+  const R ep1 = R(0.5) * (eig1 + a1), em1 = R(0.5) * (eig1 - a1);
+  const R ep2 = R(0.5) * (eig2 + a2), em2 = R(0.5) * (eig2 - a2);
+  const R ep3 = R(0.5) * (eig3 + a3), em3 = R(0.5) * (eig3 - a3);
+  const R lam[5] = {ep1 - em1, ep2 - em2, ep3 - em3, ep3 - em3, ep3 - em3};
+
+  // Left eigenvector rows times the conserved jump (MatVec5 with beta = 0).
+  const R gk = gm1 * (ke - hroe);
+  R L[5][5] = {
+      {gk + c * (c - nv), c * nu[0] - gm1 * uroe, c * nu[1] - gm1 * vroe, c * nu[2] - gm1 * wroe, gm1},
+      {gk + c * (c + nv), -c * nu[0] - gm1 * uroe, -c * nu[1] - gm1 * vroe, -c * nu[2] - gm1 * wroe, gm1},
+      {ke - hroe, -uroe, -vroe, -wroe, R(1.0)},
+      {-tv, tu[0], tu[1], tu[2], R(0.0)},
+      {-bv, bu[0], bu[1], bu[2], R(0.0)}};
+  R ldq[5];
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    R acc = R(0.0);
+#pragma unroll
+    for (int j = 0; j < 5; ++j) acc += L[i][j] * dq[j];
+    ldq[i] = lam[i] * acc;
+  }
+  const R hk = hroe + ke;
+  R M[5][5] = {
+      {hcssi, hcssi, -gm1 * cssi, R(0.0), R(0.0)},
+      {(uroe + nu[0] * c) * hcssi, (uroe - nu[0] * c) * hcssi, -gm1 * uroe * cssi, tu[0], bu[0]},
+      {(vroe + nu[1] * c) * hcssi, (vroe - nu[1] * c) * hcssi, -gm1 * vroe * cssi, tu[1], bu[1]},
+      {(wroe + nu[2] * c) * hcssi, (wroe - nu[2] * c) * hcssi, -gm1 * wroe * cssi, tu[2], bu[2]},
+      {(hk + c * nv) * hcssi, (hk - c * nv) * hcssi, (c * c - gm1 * hk) * cssi, tv, bv}};
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    R acc = R(0.0);
+#pragma unroll
+    for (int j = 0; j < 5; ++j) acc += M[i][j] * ldq[j];
+    flux[i] -= R(0.5) * acc;
+  }
+}
+
+// Gas transport: Sutherland law (reference) or constant mu with given Prandtl.
+struct Transport {
+  int model;       // 0 Sutherland, 1 constant
+  double mu;
+  double prandtl;
+};
+
+template <class R>
+__device__ __forceinline__ void transport(const Transport& tr, R T, R& mu, R& k) {
+  if (tr.model == 1) {
+    mu = R(tr.mu);
+    k = mu * R(1006.0) / R(tr.prandtl);
+  } else {
+    mu = R(1.458e-6) * T * dsqrt<R>(T) / (T + R(110.4));
+    k = mu * R(1006.0) / R(0.71);
+  }
+}
+
+// Newtonian stress and Fourier heat flux through area vector a.
+template <class R>
+__device__ __forceinline__ void viscous_flux(const R g[5][3], const R prim[5], const R a[3], const Transport& tr,
+                                             R vflux[5]) {
+  R mu, kc;
+  transport<R>(tr, prim[4], mu, kc);
+  R div = R(0);
+#pragma unroll
+  for (int i = 0; i < 5; ++i) vflux[i] = R(0.0);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) div += g[i + 1][i];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const R delta = (i == j) ? R(1) : R(0);
+      const R S = R(0.5) * (g[i + 1][j] + g[j + 1][i]);
+      const R tij = S - div * delta / R(3.);
+      vflux[1 + i] += (R(2) * mu * tij) * a[j];
+      vflux[4] += (R(2) * mu * tij) * prim[i + 1] * a[j];
+    }
+    vflux[4] += kc * g[4][i] * a[i];
+  }
+}
+
+template <class R>
+__device__ __forceinline__ R venkat(R dumax, R dumin, R du, R deltax3) {
+  const R eps2 = deltax3;  // deltax3 * beta^3 with beta = 1
+  R phi;
+  if (du > R(1e-40)) {
+    const R num = (dumax * dumax + eps2) * du + R(2) * du * du * dumax;
+    const R den = du * (dumax * dumax + R(2) * du * du + dumax * du + eps2);
+    phi = num / den;
+  } else if (du < R(-1e-40)) {
+    const R num = (dumin * dumin + eps2) * du + R(2) * du * du * dumin;
+    const R den = du * (dumin * dumin + R(2) * du * du + dumin * du + eps2);
+    phi = num / den;
+  } else {
+    phi = R(1);
+  }
+  return phi;
+}
+
+template <class R>
+__device__ __forceinline__ R vanalbada(R dumax, R dumin, R du) {
+  // The reference's threshold is DBL_EPSILON in both precisions.
+  R y = R(2);
+  if (du > R(DBL_EPSILON)) y = dumax / du;
+  else if (du < R(-DBL_EPSILON)) y = dumin / du;
+  R phi = R(1);
+  if (y < R(2)) {
+    phi = (R(4) * y - y * y) / (y * y - R(4) * y + R(8));
+    phi = (phi < R(0.0)) ? R(0.0) : phi;   // std::max(phi, 0.0)
+    phi = (R(1.0) < phi) ? R(1.0) : phi;   // std::min(phi, 1.0)
+  }
+  return phi;
+}
+
+// Ghost state with the normal velocity reflected; nn is |n| computed as
+// sqrt(((0 + n0^2) + n1^2) + n2^2), which equals the Roe |n|.
+template <class R>
+__device__ __forceinline__ void reflect_state(const R n[3], R nn, const R pl[5], R pr[5]) {
+  R ub = R(0.0);
+  ub += pl[1] * n[0] / nn;
+  ub += pl[2] * n[1] / nn;
+  ub += pl[3] * n[2] / nn;
+  pr[0] = pl[0];
+  pr[1] = pl[1] - R(2) * ub * n[0] / nn;
+  pr[2] = pl[2] - R(2) * ub * n[1] / nn;
+  pr[3] = pl[3] - R(2) * ub * n[2] / nn;
+  pr[4] = pl[4];
+}
+
+}  // namespace dev
+}  // namespace miniaero

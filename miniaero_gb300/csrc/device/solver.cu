@@ -1,0 +1,676 @@
+// Device mesh, solver objects and the device half of the C ABI.
+//
+// ma_mesh_upload turns a reference-ordered mesh (MeshData, kokkos/MeshData.h)
+// into the device layout:
+//  * internal faces re-ordered by (left, right) cell for locality; face
+//    results do not depend on the order faces are computed in;
+//  * boundary faces grouped by BC type (Extrapolate, Tangent, NoSlip, Inflow);
+//  * per-face Roe frame |n|, n/|n|, t/|t|, b/|b| and centroid offsets,
+//    computed once with the reference's expressions;
+//  * per-cell ordered contribution lists that replay the reference's serial
+//    accumulation order: internal faces in permutation order, then boundary
+//    sets in boundary_faces order (GreenGauss.h:300-321, StencilLimiter.h:532-616)
+//    or grouped by BC type (TimeSolverExplicitRK4.h:428-475) for the residual.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../../include/miniaero_gpu.h"
+#include "../host/errors.hpp"
+#include "kernels.cuh"
+
+using miniaero::set_error;
+namespace dev = miniaero::dev;
+
+#define MA_CUDA_TRY(expr)                                                                   \
+  do {                                                                                     \
+    cudaError_t err__ = (expr);                                                            \
+    if (err__ != cudaSuccess)                                                              \
+      return set_error(MA_ECUDA, std::string(#expr) + ": " + cudaGetErrorString(err__)); \
+  } while (0)
+
+namespace {
+
+// Single device allocation carved into aligned pieces.
+struct Arena {
+  char* base = nullptr;
+  size_t size = 0, used = 0;
+  template <class T>
+  T* take(size_t n) {
+    const size_t off = (used + 255) & ~size_t(255);
+    used = off + n * sizeof(T);
+    return base ? reinterpret_cast<T*>(base + off) : nullptr;
+  }
+};
+
+}  // namespace
+
+struct ma_mesh {
+  dev::TopoView topo;
+  dev::GeomView<double> g64;
+  dev::GeomView<float> g32;
+  void* dmem = nullptr;
+  size_t bytes = 0;
+  int device = 0;
+};
+
+struct ma_solver {
+  ma_mesh* mesh = nullptr;
+  ma_options opts;
+  dev::PathConfig cfg;
+  bool mixed = false;
+  cudaStream_t stream = nullptr;
+  dev::StateBuffers st;
+  dev::StageBuffers<double> b64;
+  dev::StageBuffers<float> b32;
+  void* dmem = nullptr;
+  size_t bytes = 0;
+  unsigned long long* dscratch = nullptr;  // 8-byte reduction slot
+  cudaGraphExec_t graph = nullptr;
+  bool state_set = false;
+  int64_t steps_done = 0;
+};
+
+// ---------------------------------------------------------------------------
+extern "C" int32_t ma_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+namespace {
+
+ma_status validate_view(const ma_mesh_view* v) {
+  if (!v) return set_error(MA_EINVAL, "mesh view is null");
+  if (v->ncells <= 0) return set_error(MA_EINVAL, "mesh has no cells");
+  if (!v->cell_coords || !v->cell_volumes) return set_error(MA_EINVAL, "mesh cell arrays are null");
+  if (v->nbc < 0 || v->nbc > MA_MAX_BC_SETS) return set_error(MA_EINVAL, "bad boundary set count");
+  auto check_set = [&](const ma_face_set& s, bool internal) -> ma_status {
+    if (s.nfaces < 0) return set_error(MA_EINVAL, "negative face count");
+    if (s.nfaces == 0) return MA_OK;
+    if (!s.conn || !s.coords || !s.normal || !s.tangent || !s.binormal || !s.permutation)
+      return set_error(MA_EINVAL, "face set has null arrays");
+    if (!internal && (s.type < 0 || s.type > 3)) return set_error(MA_EINVAL, "unknown boundary condition type");
+    std::vector<char> seen(static_cast<size_t>(s.nfaces), 0);
+    for (int32_t i = 0; i < s.nfaces; ++i) {
+      const int32_t p = s.permutation[i];
+      if (p < 0 || p >= s.nfaces || seen[p]) return set_error(MA_EINVAL, "face permutation is not a permutation");
+      seen[p] = 1;
+      const int32_t L = s.conn[2 * i], R = s.conn[2 * i + 1];
+      if (L < 0 || L >= v->ncells) return set_error(MA_EINVAL, "face left cell out of range");
+      if (internal && (R < 0 || R >= v->ncells || R == L)) return set_error(MA_EINVAL, "internal face right cell out of range");
+    }
+    return MA_OK;
+  };
+  ma_status st = check_set(v->internal, true);
+  if (st != MA_OK) return st;
+  for (int b = 0; b < v->nbc; ++b) {
+    st = check_set(v->bc[b], false);
+    if (st != MA_OK) return st;
+  }
+  for (int32_t c = 0; c < v->ncells; ++c)
+    if (!(v->cell_volumes[c] > 0.0)) return set_error(MA_EINVAL, "non-positive cell volume");
+  return MA_OK;
+}
+
+// Position of a BC type in the residual order Extrapolate, Tangent, NoSlip, Inflow.
+inline int type_rank(int type) {
+  switch (type) {
+    case MA_BC_EXTRAPOLATE: return 0;
+    case MA_BC_TANGENT: return 1;
+    case MA_BC_NOSLIP: return 2;
+    default: return 3;
+  }
+}
+
+}  // namespace
+
+extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
+  if (!out) return set_error(MA_EINVAL, "ma_mesh_upload: out is null");
+  *out = nullptr;
+  ma_status st = validate_view(v);
+  if (st != MA_OK) return st;
+  try {
+    const int32_t C = v->ncells;
+    const int32_t Fi = v->internal.nfaces;
+    int64_t Fb64 = 0;
+    for (int b = 0; b < v->nbc; ++b) Fb64 += v->bc[b].nfaces;
+    if (static_cast<int64_t>(Fi) + Fb64 >= (1LL << 30)) return set_error(MA_EINVAL, "too many faces");
+    const int32_t Fb = static_cast<int32_t>(Fb64);
+    const int32_t F = Fi + Fb;
+
+    // Device order of internal faces: by (left, right), two stable counting sorts.
+    std::vector<int32_t> order(Fi), tmp(Fi), cnt(static_cast<size_t>(C) + 1);
+    {
+      const int32_t* conn = v->internal.conn;
+      auto pass = [&](const std::vector<int32_t>& in, std::vector<int32_t>& outv, int side) {
+        std::fill(cnt.begin(), cnt.end(), 0);
+        for (int32_t i : in) cnt[conn[2 * i + side] + 1]++;
+        for (int32_t c = 0; c < C; ++c) cnt[c + 1] += cnt[c];
+        for (int32_t i : in) outv[cnt[conn[2 * i + side]]++] = i;
+      };
+      for (int32_t i = 0; i < Fi; ++i) tmp[i] = i;
+      pass(tmp, order, 1);
+      pass(order, tmp, 0);
+      order.swap(tmp);
+    }
+    std::vector<int32_t> gpu_of_internal(Fi);
+    for (int32_t g = 0; g < Fi; ++g) gpu_of_internal[order[g]] = g;
+
+    // Boundary faces grouped by type rank, then set order, then storage order.
+    std::vector<int32_t> bc_base(v->nbc, 0);
+    int32_t nbc_type[4] = {0, 0, 0, 0};
+    {
+      int32_t pos = Fi;
+      for (int r = 0; r < 4; ++r)
+        for (int b = 0; b < v->nbc; ++b)
+          if (type_rank(v->bc[b].type) == r) {
+            bc_base[b] = pos;
+            pos += v->bc[b].nfaces;
+            nbc_type[r] += v->bc[b].nfaces;
+          }
+    }
+
+    // Host staging of face data in device order.
+    std::vector<int32_t> fconn(2 * static_cast<size_t>(F));
+    std::vector<double> geo(19 * static_cast<size_t>(F), 0.0);  // fn3 fnu3 ftu3 fbu3 fnn1 dL3 dR3
+    auto put_face = [&](int32_t g, const ma_face_set& s, int32_t i, bool internal) {
+      const int32_t L = s.conn[2 * i];
+      const int32_t R = internal ? s.conn[2 * i + 1] : -1;
+      fconn[g] = L;
+      fconn[static_cast<size_t>(F) + g] = R;
+      const double* n = &s.normal[3 * static_cast<size_t>(i)];
+      const double* t = &s.tangent[3 * static_cast<size_t>(i)];
+      const double* b = &s.binormal[3 * static_cast<size_t>(i)];
+      const double* x = &s.coords[3 * static_cast<size_t>(i)];
+      // Roe_Flux.h:100-118
+      const double nn = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+      const double tn = std::sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+      const double bn = std::sqrt(b[0] * b[0] + b[1] * b[1] + b[2] * b[2]);
+      for (int d = 0; d < 3; ++d) {
+        geo[(0 + d) * static_cast<size_t>(F) + g] = n[d];
+        geo[(3 + d) * static_cast<size_t>(F) + g] = n[d] / nn;
+        geo[(6 + d) * static_cast<size_t>(F) + g] = t[d] / tn;
+        geo[(9 + d) * static_cast<size_t>(F) + g] = b[d] / bn;
+        geo[(13 + d) * static_cast<size_t>(F) + g] = x[d] - v->cell_coords[3 * static_cast<size_t>(L) + d];
+        if (internal) geo[(16 + d) * static_cast<size_t>(F) + g] = x[d] - v->cell_coords[3 * static_cast<size_t>(R) + d];
+      }
+      geo[12 * static_cast<size_t>(F) + g] = nn;
+    };
+    for (int32_t i = 0; i < Fi; ++i) put_face(gpu_of_internal[i], v->internal, i, true);
+    for (int b = 0; b < v->nbc; ++b)
+      for (int32_t i = 0; i < v->bc[b].nfaces; ++i) put_face(bc_base[b] + i, v->bc[b], i, false);
+
+    // Ordered per-cell contribution lists.
+    const size_t K = dev::kMaxCellFaces;
+    std::vector<int32_t> csr_grad(K * C, -1), csr_nbr(K * C, -1), csr_flux(K * C, -1);
+    std::vector<uint8_t> ng(C, 0), nf(C, 0);
+    bool overflow = false;
+    auto push = [&](std::vector<int32_t>& csr, std::vector<uint8_t>& n, int32_t cell, int32_t code, int32_t nbr,
+                    bool with_nbr) {
+      if (n[cell] >= K) { overflow = true; return; }
+      csr[n[cell] * static_cast<size_t>(C) + cell] = code;
+      if (with_nbr) csr_nbr[n[cell] * static_cast<size_t>(C) + cell] = nbr;
+      n[cell]++;
+    };
+    for (int32_t ii = 0; ii < Fi; ++ii) {
+      const int32_t i = v->internal.permutation[ii];
+      const int32_t g = gpu_of_internal[i];
+      const int32_t L = v->internal.conn[2 * i], R = v->internal.conn[2 * i + 1];
+      push(csr_grad, ng, L, (g << 1) | 1, R, true);
+      push(csr_grad, ng, R, (g << 1), L, true);
+      push(csr_flux, nf, L, (g << 1) | 1, 0, false);
+      push(csr_flux, nf, R, (g << 1), 0, false);
+    }
+    for (int b = 0; b < v->nbc; ++b)  // boundary_faces order
+      for (int32_t i = 0; i < v->bc[b].nfaces; ++i)
+        push(csr_grad, ng, v->bc[b].conn[2 * i], ((bc_base[b] + i) << 1) | 1, -1, true);
+    for (int r = 0; r < 4; ++r)  // grouped by BC type
+      for (int b = 0; b < v->nbc; ++b)
+        if (type_rank(v->bc[b].type) == r)
+          for (int32_t i = 0; i < v->bc[b].nfaces; ++i)
+            push(csr_flux, nf, v->bc[b].conn[2 * i], ((bc_base[b] + i) << 1) | 1, 0, false);
+    if (overflow) return set_error(MA_EINVAL, "a cell has more than 6 faces");
+
+    // Device arena.
+    Arena a;
+    auto layout = [&](ma_mesh& m) {
+      m.topo.vol = a.take<double>(C);
+      m.topo.fconn = a.take<int32_t>(2 * static_cast<size_t>(F));
+      m.topo.csr_grad = a.take<int32_t>(K * C);
+      m.topo.csr_nbr = a.take<int32_t>(K * C);
+      m.topo.csr_flux = a.take<int32_t>(K * C);
+      double* g64 = a.take<double>(19 * static_cast<size_t>(F));
+      float* g32 = a.take<float>(19 * static_cast<size_t>(F));
+      double* vol64 = const_cast<double*>(m.topo.vol);
+      float* vol32 = a.take<float>(C);
+      auto assign = [&](auto& gv, auto* base, auto* vol) {
+        gv.vol = vol;
+        gv.fn = base;
+        gv.fnu = base + 3 * static_cast<size_t>(F);
+        gv.ftu = base + 6 * static_cast<size_t>(F);
+        gv.fbu = base + 9 * static_cast<size_t>(F);
+        gv.fnn = base + 12 * static_cast<size_t>(F);
+        gv.dL = base + 13 * static_cast<size_t>(F);
+        gv.dR = base + 16 * static_cast<size_t>(F);
+      };
+      assign(m.g64, g64, vol64);
+      assign(m.g32, g32, vol32);
+    };
+    ma_mesh probe;
+    layout(probe);
+    const size_t bytes = a.used;
+    a.used = 0;
+    MA_CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&a.base), bytes));
+    ma_mesh* m = new ma_mesh;
+    layout(*m);
+    m->dmem = a.base;
+    m->bytes = bytes;
+    cudaGetDevice(&m->device);
+    m->topo.C = C;
+    m->topo.Fi = Fi;
+    m->topo.Fb = Fb;
+    m->topo.F = F;
+    for (int r = 0; r < 4; ++r) m->topo.nbc_type[r] = nbc_type[r];
+
+    std::vector<float> geo32(geo.size());
+    for (size_t i = 0; i < geo.size(); ++i) geo32[i] = static_cast<float>(geo[i]);
+    std::vector<float> vol32(C);
+    for (int32_t c = 0; c < C; ++c) vol32[c] = static_cast<float>(v->cell_volumes[c]);
+    auto copy = [&](const void* dst, const void* src, size_t n) {
+      return cudaMemcpy(const_cast<void*>(dst), src, n, cudaMemcpyHostToDevice);
+    };
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = copy(m->topo.vol, v->cell_volumes, sizeof(double) * C);
+    if (e == cudaSuccess) e = copy(m->topo.fconn, fconn.data(), sizeof(int32_t) * fconn.size());
+    if (e == cudaSuccess) e = copy(m->topo.csr_grad, csr_grad.data(), sizeof(int32_t) * csr_grad.size());
+    if (e == cudaSuccess) e = copy(m->topo.csr_nbr, csr_nbr.data(), sizeof(int32_t) * csr_nbr.size());
+    if (e == cudaSuccess) e = copy(m->topo.csr_flux, csr_flux.data(), sizeof(int32_t) * csr_flux.size());
+    if (e == cudaSuccess) e = copy(m->g64.fn, geo.data(), sizeof(double) * geo.size());
+    if (e == cudaSuccess) e = copy(m->g32.fn, geo32.data(), sizeof(float) * geo32.size());
+    if (e == cudaSuccess) e = copy(m->g32.vol, vol32.data(), sizeof(float) * vol32.size());
+    if (e != cudaSuccess) {
+      cudaFree(m->dmem);
+      delete m;
+      return set_error(MA_ECUDA, std::string("ma_mesh_upload: ") + cudaGetErrorString(e));
+    }
+    *out = m;
+    return MA_OK;
+  } catch (const std::bad_alloc&) {
+    return set_error(MA_ENOMEM, "ma_mesh_upload: out of host memory");
+  }
+}
+
+extern "C" void ma_mesh_free(ma_mesh* m) {
+  if (!m) return;
+  cudaFree(m->dmem);
+  delete m;
+}
+
+extern "C" size_t ma_mesh_device_bytes(const ma_mesh* m) { return m ? m->bytes : 0; }
+
+// ---------------------------------------------------------------------------
+namespace {
+
+ma_status capture_step_graph(ma_solver* s) {
+  if (s->graph) {
+    cudaGraphExecDestroy(s->graph);
+    s->graph = nullptr;
+  }
+  cudaGraph_t g = nullptr;
+  MA_CUDA_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaSuccess;
+  for (int stage = 0; stage < 4 && e == cudaSuccess; ++stage) {
+    if (s->mixed)
+      e = dev::launch_stage<float>(s->mesh->topo, s->mesh->g32, s->cfg, s->st, s->b32, stage, s->stream);
+    else
+      e = dev::launch_stage<double>(s->mesh->topo, s->mesh->g64, s->cfg, s->st, s->b64, stage, s->stream);
+  }
+  cudaError_t e2 = cudaStreamEndCapture(s->stream, &g);
+  if (e != cudaSuccess || e2 != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return set_error(MA_ECUDA, std::string("step capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+  }
+  e = cudaGraphInstantiate(&s->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return set_error(MA_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  return MA_OK;
+}
+
+// dt = cfl * min_c V_c / sum_f (|u.n| + c |n|) on the current U_n.
+__global__ void k_cfl(dev::TopoView t, dev::GeomView<double> g, const double* __restrict__ Un,
+                      unsigned long long* out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= t.C) return;
+  const int C = t.C, F = t.F;
+  double U[5], V[5];
+  for (int k = 0; k < 5; ++k) U[k] = Un[k * C + c];
+  dev::primitives(U, V);
+  const double a = sqrt(1.4 * 287.05 * V[4]);
+  double sum = 0.0;
+  for (int s = 0; s < dev::kMaxCellFaces; ++s) {
+    const int code = t.csr_grad[s * C + c];
+    if (code < 0) continue;
+    const int f = code >> 1;
+    const double un = V[1] * g.fn[f] + V[2] * g.fn[F + f] + V[3] * g.fn[2 * F + f];
+    sum += fabs(un) + a * g.fnn[f];
+  }
+  const double r = t.vol[c] / sum;
+  if (r > 0.0) atomicMin(out, static_cast<unsigned long long>(__double_as_longlong(r)));
+}
+
+}  // namespace
+
+extern "C" ma_status ma_solver_create(ma_mesh* mesh, const ma_options* o, ma_solver** out) {
+  if (!mesh || !o || !out) return set_error(MA_EINVAL, "ma_solver_create: null argument");
+  *out = nullptr;
+  if (o->precision != MA_PREC_FP64 && o->precision != MA_PREC_MIXED) return set_error(MA_EINVAL, "bad precision");
+  if (o->limiter != MA_LIMITER_VENKAT && o->limiter != MA_LIMITER_VANALBADA) return set_error(MA_EINVAL, "bad limiter");
+  if (o->viscosity_model != MA_VISC_SUTHERLAND && o->viscosity_model != MA_VISC_CONSTANT)
+    return set_error(MA_EINVAL, "bad viscosity model");
+  if (o->viscosity_model == MA_VISC_CONSTANT && !(o->mu >= 0.0 && o->prandtl > 0.0))
+    return set_error(MA_EINVAL, "constant viscosity needs mu >= 0 and prandtl > 0");
+  if (!(o->cfl > 0.0) && !(o->dt > 0.0)) return set_error(MA_EINVAL, "dt must be > 0 (or cfl > 0)");
+  ma_solver* s = new (std::nothrow) ma_solver;
+  if (!s) return set_error(MA_ENOMEM, "ma_solver_create: out of host memory");
+  s->mesh = mesh;
+  s->opts = *o;
+  s->mixed = o->precision == MA_PREC_MIXED;
+  s->cfg.second_order = o->second_order_space != 0;
+  s->cfg.viscous = o->viscous != 0;
+  s->cfg.limiter = o->limiter;
+  s->cfg.transport = dev::Transport{o->viscosity_model, o->mu, o->prandtl};
+  for (int k = 0; k < 5; ++k) s->cfg.inflow[k] = o->inflow_state[k];
+  s->cfg.dt = o->dt;
+  const size_t C = mesh->topo.C, F = mesh->topo.F;
+  Arena a;
+  auto layout = [&]() {
+    s->st.Un = a.take<double>(5 * C);
+    s->st.Unp1 = a.take<double>(5 * C);
+    s->st.res = o->keep_residual ? a.take<double>(5 * C) : nullptr;
+    s->dscratch = a.take<unsigned long long>(1);
+    if (s->mixed) {
+      s->b32.W = a.take<float>(5 * C);
+      s->b32.grad = a.take<float>(15 * C);
+      s->b32.phi = a.take<float>(5 * C);
+      s->b32.fflux = a.take<float>(5 * F);
+    } else {
+      s->b64.W = a.take<double>(5 * C);
+      s->b64.grad = a.take<double>(15 * C);
+      s->b64.phi = a.take<double>(5 * C);
+      s->b64.fflux = a.take<double>(5 * F);
+    }
+  };
+  layout();
+  const size_t bytes = a.used;
+  a.used = 0;
+  cudaError_t e = cudaSetDevice(mesh->device);
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&a.base), bytes);
+  if (e != cudaSuccess) {
+    delete s;
+    cudaGetLastError();
+    return set_error(e == cudaErrorMemoryAllocation ? MA_ENOMEM : MA_ECUDA,
+                     std::string("ma_solver_create: ") + cudaGetErrorString(e));
+  }
+  layout();
+  s->dmem = a.base;
+  s->bytes = bytes;
+  e = cudaMemset(s->dmem, 0, bytes);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    cudaFree(s->dmem);
+    delete s;
+    return set_error(MA_ECUDA, std::string("ma_solver_create: ") + cudaGetErrorString(e));
+  }
+  *out = s;
+  return MA_OK;
+}
+
+extern "C" void ma_solver_free(ma_solver* s) {
+  if (!s) return;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  cudaFree(s->dmem);
+  delete s;
+}
+
+namespace {
+
+// Copies U (AOS or SOA host layout) into the device SOA array.
+ma_status upload_state(ma_solver* s, const double* U, int32_t layout) {
+  const size_t C = s->mesh->topo.C;
+  if (layout == MA_LAYOUT_SOA) {
+    MA_CUDA_TRY(cudaMemcpyAsync(s->st.Un, U, sizeof(double) * 5 * C, cudaMemcpyHostToDevice, s->stream));
+  } else if (layout == MA_LAYOUT_AOS) {
+    std::vector<double> soa(5 * C);
+    for (size_t c = 0; c < C; ++c)
+      for (int k = 0; k < 5; ++k) soa[k * C + c] = U[5 * c + k];
+    MA_CUDA_TRY(cudaMemcpyAsync(s->st.Un, soa.data(), sizeof(double) * 5 * C, cudaMemcpyHostToDevice, s->stream));
+    MA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  } else {
+    return set_error(MA_EINVAL, "unknown state layout");
+  }
+  return MA_OK;
+}
+
+ma_status download(ma_solver* s, const double* src, double* U, int32_t layout) {
+  const size_t C = s->mesh->topo.C;
+  if (layout == MA_LAYOUT_SOA) {
+    MA_CUDA_TRY(cudaMemcpyAsync(U, src, sizeof(double) * 5 * C, cudaMemcpyDeviceToHost, s->stream));
+    MA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  } else if (layout == MA_LAYOUT_AOS) {
+    std::vector<double> soa(5 * C);
+    MA_CUDA_TRY(cudaMemcpyAsync(soa.data(), src, sizeof(double) * 5 * C, cudaMemcpyDeviceToHost, s->stream));
+    MA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    for (size_t c = 0; c < C; ++c)
+      for (int k = 0; k < 5; ++k) U[5 * c + k] = soa[k * C + c];
+  } else {
+    return set_error(MA_EINVAL, "unknown state layout");
+  }
+  return MA_OK;
+}
+
+}  // namespace
+
+extern "C" ma_status ma_solver_set_state(ma_solver* s, const double* U, int32_t layout) {
+  if (!s || !U) return set_error(MA_EINVAL, "ma_solver_set_state: null argument");
+  MA_CUDA_TRY(cudaSetDevice(s->mesh->device));
+  ma_status st = upload_state(s, U, layout);
+  if (st != MA_OK) return st;
+  const dev::TopoView& t = s->mesh->topo;
+  if (s->opts.cfl > 0.0) {
+    MA_CUDA_TRY(cudaMemsetAsync(s->dscratch, 0xff, sizeof(unsigned long long), s->stream));
+    k_cfl<<<(t.C + 255) / 256, 256, 0, s->stream>>>(t, s->mesh->g64, s->st.Un, s->dscratch);
+    MA_CUDA_TRY(cudaGetLastError());
+    unsigned long long bits = 0;
+    MA_CUDA_TRY(cudaMemcpyAsync(&bits, s->dscratch, sizeof(bits), cudaMemcpyDeviceToHost, s->stream));
+    MA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    double r;
+    std::memcpy(&r, &bits, sizeof(r));
+    if (!(r > 0.0) || !std::isfinite(r)) return set_error(MA_ENUMERIC, "CFL time step is not finite");
+    s->cfg.dt = s->opts.cfl * r;
+    if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
+  }
+  if (s->mixed)
+    MA_CUDA_TRY(dev::launch_init_primitives<float>(t, s->st, s->b32, s->stream));
+  else
+    MA_CUDA_TRY(dev::launch_init_primitives<double>(t, s->st, s->b64, s->stream));
+  if (s->st.res) MA_CUDA_TRY(cudaMemsetAsync(s->st.res, 0, sizeof(double) * 5 * t.C, s->stream));
+  MA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  s->state_set = true;
+  s->steps_done = 0;
+  return MA_OK;
+}
+
+extern "C" ma_status ma_solver_init_state(ma_solver* s, const ma_host_mesh* hm) {
+  if (!s || !hm) return set_error(MA_EINVAL, "ma_solver_init_state: null argument");
+  std::vector<double> U(5 * static_cast<size_t>(s->mesh->topo.C));
+  ma_status st = ma_host_initial_state(hm, &s->opts, U.data());
+  if (st != MA_OK) return st;
+  return ma_solver_set_state(s, U.data(), MA_LAYOUT_AOS);
+}
+
+extern "C" ma_status ma_solver_get_state(ma_solver* s, double* U, int32_t layout) {
+  if (!s || !U) return set_error(MA_EINVAL, "ma_solver_get_state: null argument");
+  if (!s->state_set) return set_error(MA_ESTATE, "solver state has not been set");
+  MA_CUDA_TRY(cudaSetDevice(s->mesh->device));
+  return download(s, s->st.Un, U, layout);
+}
+
+extern "C" ma_status ma_solver_get_residual(ma_solver* s, double* res, int32_t layout) {
+  if (!s || !res) return set_error(MA_EINVAL, "ma_solver_get_residual: null argument");
+  if (!s->st.res) return set_error(MA_ESTATE, "solver was created without keep_residual");
+  MA_CUDA_TRY(cudaSetDevice(s->mesh->device));
+  return download(s, s->st.res, res, layout);
+}
+
+extern "C" ma_status ma_solver_step(ma_solver* s, int32_t nsteps) {
+  if (!s) return set_error(MA_EINVAL, "ma_solver_step: null solver");
+  if (nsteps < 0) return set_error(MA_EINVAL, "ma_solver_step: negative step count");
+  if (!s->state_set) return set_error(MA_ESTATE, "solver state has not been set");
+  if (nsteps == 0) return MA_OK;
+  MA_CUDA_TRY(cudaSetDevice(s->mesh->device));
+  if (!s->graph) {
+    ma_status st = capture_step_graph(s);
+    if (st != MA_OK) return st;
+  }
+  for (int32_t i = 0; i < nsteps; ++i) MA_CUDA_TRY(cudaGraphLaunch(s->graph, s->stream));
+  s->steps_done += nsteps;
+  return MA_OK;
+}
+
+extern "C" ma_status ma_solver_synchronize(ma_solver* s) {
+  if (!s) return set_error(MA_EINVAL, "ma_solver_synchronize: null solver");
+  MA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return MA_OK;
+}
+
+extern "C" void* ma_solver_stream(ma_solver* s) { return s ? static_cast<void*>(s->stream) : nullptr; }
+extern "C" double ma_solver_dt(const ma_solver* s) { return s ? s->cfg.dt : 0.0; }
+extern "C" int64_t ma_solver_steps_done(const ma_solver* s) { return s ? s->steps_done : 0; }
+
+extern "C" int32_t ma_solver_launches_per_step(const ma_solver* s) {
+  return s ? 4 * dev::launches_per_stage(s->cfg, s->mesh->topo) : 0;
+}
+
+extern "C" ma_status ma_solver_set_dt(ma_solver* s, double dt) {
+  if (!s || !(dt > 0.0)) return set_error(MA_EINVAL, "ma_solver_set_dt: dt must be > 0");
+  s->cfg.dt = dt;
+  if (s->graph) {
+    cudaGraphExecDestroy(s->graph);
+    s->graph = nullptr;
+  }
+  return MA_OK;
+}
+
+extern "C" ma_status ma_solver_check_state(ma_solver* s, int64_t* bad_cell) {
+  if (!s) return set_error(MA_EINVAL, "ma_solver_check_state: null solver");
+  if (bad_cell) *bad_cell = -1;
+  MA_CUDA_TRY(cudaSetDevice(s->mesh->device));
+  MA_CUDA_TRY(cudaMemsetAsync(s->dscratch, 0xff, sizeof(unsigned long long), s->stream));
+  MA_CUDA_TRY(dev::launch_check_state(s->mesh->topo.C, s->st.Un, s->dscratch, s->stream));
+  unsigned long long first = 0;
+  MA_CUDA_TRY(cudaMemcpyAsync(&first, s->dscratch, sizeof(first), cudaMemcpyDeviceToHost, s->stream));
+  MA_CUDA_TRY(cudaStreamSynchronize(s->stream));
+  if (first != ~0ULL) {
+    if (bad_cell) *bad_cell = static_cast<int64_t>(first);
+    return set_error(MA_ENUMERIC, "non-finite or non-positive state at cell " + std::to_string(first));
+  }
+  return MA_OK;
+}
+
+extern "C" ma_status ma_solver_solve(ma_solver* s, const ma_host_mesh* hm) {
+  ma_status st = ma_solver_init_state(s, hm);
+  if (st != MA_OK) return st;
+  st = ma_solver_step(s, s->opts.ntimesteps);
+  if (st != MA_OK) return st;
+  return ma_solver_synchronize(s);
+}
+
+// ---------------------------------------------------------------------------
+// Operator-level entry points: host arrays in, host arrays out.
+namespace {
+
+struct DevBufs {
+  std::vector<void*> ptrs;
+  ~DevBufs() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+  cudaError_t in(const double* h, size_t n, double** d) {
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(d), sizeof(double) * (n ? n : 1));
+    if (e != cudaSuccess) return e;
+    ptrs.push_back(*d);
+    return h ? cudaMemcpy(*d, h, sizeof(double) * n, cudaMemcpyHostToDevice) : cudaSuccess;
+  }
+};
+
+}  // namespace
+
+extern "C" ma_status ma_op_roe_flux(int32_t n, const double* pl, const double* pr, const double* normal,
+                                    const double* tangent, const double* binormal, double* flux) {
+  if (n < 0 || (n > 0 && (!pl || !pr || !normal || !tangent || !binormal || !flux)))
+    return set_error(MA_EINVAL, "ma_op_roe_flux: bad arguments");
+  if (n == 0) return MA_OK;
+  DevBufs b;
+  double *dpl, *dpr, *dn, *dt, *db, *df;
+  MA_CUDA_TRY(b.in(pl, 5 * (size_t)n, &dpl));
+  MA_CUDA_TRY(b.in(pr, 5 * (size_t)n, &dpr));
+  MA_CUDA_TRY(b.in(normal, 3 * (size_t)n, &dn));
+  MA_CUDA_TRY(b.in(tangent, 3 * (size_t)n, &dt));
+  MA_CUDA_TRY(b.in(binormal, 3 * (size_t)n, &db));
+  MA_CUDA_TRY(b.in(nullptr, 5 * (size_t)n, &df));
+  MA_CUDA_TRY(dev::launch_op_roe(n, dpl, dpr, dn, dt, db, df, 0));
+  MA_CUDA_TRY(cudaMemcpy(flux, df, sizeof(double) * 5 * n, cudaMemcpyDeviceToHost));
+  return MA_OK;
+}
+
+extern "C" ma_status ma_op_viscous_flux(int32_t n, const double* grad, const double* prim, const double* area,
+                                        int32_t viscosity_model, double mu, double prandtl, double* vflux) {
+  if (n < 0 || (n > 0 && (!grad || !prim || !area || !vflux))) return set_error(MA_EINVAL, "ma_op_viscous_flux: bad arguments");
+  if (n == 0) return MA_OK;
+  DevBufs b;
+  double *dg, *dp, *da, *dv;
+  MA_CUDA_TRY(b.in(grad, 15 * (size_t)n, &dg));
+  MA_CUDA_TRY(b.in(prim, 5 * (size_t)n, &dp));
+  MA_CUDA_TRY(b.in(area, 3 * (size_t)n, &da));
+  MA_CUDA_TRY(b.in(nullptr, 5 * (size_t)n, &dv));
+  MA_CUDA_TRY(dev::launch_op_viscous(n, dg, dp, da, dev::Transport{viscosity_model, mu, prandtl}, dv, 0));
+  MA_CUDA_TRY(cudaMemcpy(vflux, dv, sizeof(double) * 5 * n, cudaMemcpyDeviceToHost));
+  return MA_OK;
+}
+
+extern "C" ma_status ma_op_limiter(int32_t n, int32_t kind, const double* dumax, const double* dumin,
+                                   const double* du, const double* d2, double* phi) {
+  if (n < 0 || (n > 0 && (!dumax || !dumin || !du || !phi || (kind == 0 && !d2))) || kind < 0 || kind > 1)
+    return set_error(MA_EINVAL, "ma_op_limiter: bad arguments");
+  if (n == 0) return MA_OK;
+  DevBufs b;
+  double *a, *bb, *c, *d, *p;
+  MA_CUDA_TRY(b.in(dumax, n, &a));
+  MA_CUDA_TRY(b.in(dumin, n, &bb));
+  MA_CUDA_TRY(b.in(du, n, &c));
+  MA_CUDA_TRY(b.in(d2, d2 ? n : 0, &d));
+  MA_CUDA_TRY(b.in(nullptr, n, &p));
+  MA_CUDA_TRY(dev::launch_op_limiter(n, kind, a, bb, c, d, p, 0));
+  MA_CUDA_TRY(cudaMemcpy(phi, p, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  return MA_OK;
+}
+
+extern "C" ma_status ma_op_primitives(int32_t n, const double* U, double* V) {
+  if (n < 0 || (n > 0 && (!U || !V))) return set_error(MA_EINVAL, "ma_op_primitives: bad arguments");
+  if (n == 0) return MA_OK;
+  DevBufs b;
+  double *du, *dv;
+  MA_CUDA_TRY(b.in(U, 5 * (size_t)n, &du));
+  MA_CUDA_TRY(b.in(nullptr, 5 * (size_t)n, &dv));
+  MA_CUDA_TRY(dev::launch_op_primitives(n, du, dv, 0));
+  MA_CUDA_TRY(cudaMemcpy(V, dv, sizeof(double) * 5 * n, cudaMemcpyDeviceToHost));
+  return MA_OK;
+}

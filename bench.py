@@ -1,0 +1,416 @@
+"""Benchmark of the RK4 residual path on one GB300 (or N replicas).
+
+Workload (default, N=1): Sod shock tube at scale, 256x128x128 Hexa8 cells
+(4,194,304) on 1.0x0.5x0.5, rho/p = 1/1 | 0.125/0.1, second order with
+Green-Gauss gradients and the Venkatakrishnan limiter, viscous (constant
+mu = 1.8e-5, Pr = 0.72), dt from CFL 0.5 at t = 0, plain FP64. A "step" is one
+RK4 time step (4 stages) over the whole mesh; the unit of work is one
+cell-stage, metric Mcell-stage/s = cells * 4 * steps / seconds / 1e6.
+
+Timing: W warm-up steps, then K steps as CUDA graph launches bracketed by a
+barrier and device synchronisation, timed with CUDA events on the solver's
+stream. Working set (state, gradients, face data) is ~3 GB, far above the
+129 MB L2. The mixed form (FP32 flux/gradient/limiter, FP64 accumulation and
+RK update) is measured on the same mesh and reported with its error against
+the FP64 result. The end-to-end figure times, per step, the host->device copy
+of the state from pinned memory, the step and the device->host copy of the
+result, all through the C ABI.
+
+--impl reference times the CPU restatement of the reference's Kokkos OpenMP
+loops (oracle port, all host threads) on the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+WORKLOADS = {
+    # name: options, description
+    "sod_2nd_viscous_256x128x128": dict(
+        problem_type=0, lx=1.0, ly=0.5, lz=0.5, nx=256, ny=128, nz=128, second_order_space=1, viscous=1,
+        viscosity_model=1, mu=1.8e-5, prandtl=0.72, ic=1, sod_left=[1.0, 1.0], sod_right=[0.125, 0.1], cfl=0.5,
+        ntimesteps=100),
+    "sod_1st_inviscid_128x16x16": dict(
+        problem_type=0, lx=1.0, ly=0.1, lz=0.1, nx=128, ny=16, nz=16, second_order_space=0, viscous=0,
+        ic=1, sod_left=[1.0, 1.0], sod_right=[0.125, 0.1], dt=1e-5, ntimesteps=200),
+    # Same physics as the default at 262,144 cells: small case for ncu captures.
+    "sod_2nd_viscous_64x64x64": dict(
+        problem_type=0, lx=1.0, ly=0.5, lz=0.5, nx=64, ny=64, nz=64, second_order_space=1, viscous=1,
+        viscosity_model=1, mu=1.8e-5, prandtl=0.72, ic=1, sod_left=[1.0, 1.0], sod_right=[0.125, 0.1], cfl=0.5,
+        ntimesteps=100),
+    "flat_plate_vanalbada_512x128x128": dict(
+        problem_type=1, lx=2.0, ly=0.5, lz=0.5, nx=512, ny=128, nz=128, second_order_space=1, viscous=1,
+        limiter=1, viscosity_model=1, mu=1.8e-5, prandtl=0.72, ic=2, cfl=0.5, ntimesteps=50),
+}
+DEFAULT_WORKLOAD = "sod_2nd_viscous_256x128x128"
+
+# Algorithmic (compulsory) DRAM bytes per launch, FP64 second-order viscous:
+# each array read or written once per launch. Per internal face of the flux
+# kernel: conn 8 + area vector, unit n/t/b, |n| 104 + centroid offsets 48 +
+# flux write 40 = 200 B; per cell it reads W 40 + grad 120 + phi 40 = 200 B.
+FLUX_BYTES_PER_FACE = 200
+FLUX_BYTES_PER_CELL = 200
+
+
+def flat_plate_inflow(mach=0.3, T=300.0, p=1e5):
+    R, g = 287.05, 1.4
+    rho = p / (R * T)
+    u = mach * (g * R * T) ** 0.5
+    return [rho, rho * u, 0.0, 0.0, rho * (R / (g - 1.0) * T + 0.5 * u * u)]
+
+
+def make_options(ma, name, precision="fp64"):
+    kw = dict(WORKLOADS[name])
+    o = ma.Options(**kw)
+    if name.startswith("flat_plate"):
+        o.inflow_state = flat_plate_inflow()
+        o.inflow_given = 1
+    o.precision = ma.MA_PREC_MIXED if precision == "mixed" else ma.MA_PREC_FP64
+    return o
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle-reason sampling during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def load_traffic(kernel):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(kernel)
+    except Exception:
+        return None
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl != "reference" else "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(world, value):
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline_sample(ma, oracle, md, o, U0, dt, seconds=15.0, nthreads=None):
+    """Times the oracle port (OpenMP, all host threads) on whole-mesh steps."""
+    nthreads = nthreads or os.cpu_count() or 1
+    st = oracle.Stepper(md, o, U0, dt=dt, nthreads=nthreads)
+    t0 = time.perf_counter()
+    st.step(1)
+    t1 = time.perf_counter()
+    per_step = t1 - t0
+    nsteps = max(1, min(20, int(seconds / max(per_step, 1e-6))))
+    t0 = time.perf_counter()
+    st.step(nsteps)
+    elapsed = time.perf_counter() - t0
+    st.close()
+    value = md.ncells * 4 * nsteps / elapsed / 1e6
+    return {"value": value, "unit": "Mcell-stage/s", "cores": nthreads, "kind": "port",
+            "sample": "%d RK4 steps of the full %d-cell mesh after 1 untimed step (%.1f s)"
+                      % (nsteps, md.ncells, elapsed)}
+
+
+def run_reference(args, world, rank):
+    import miniaero_gb300 as ma
+    import oracle
+    if rank != 0:
+        return
+    name = args.workload
+    o = make_options(ma, name)
+    md = ma.Parallel3DMesh.from_options(o).fill_mesh_data()
+    U0 = ma.initial_state(md, o)
+    dt = o.dt
+    if o.cfl > 0:
+        dt = cfl_dt_host(md, U0, o.cfl)
+    nthreads = os.cpu_count() or 1
+    st = oracle.Stepper(md, o, U0, dt=dt, nthreads=nthreads)
+    st.step(args.warmup)
+    t0 = time.perf_counter()
+    st.step(args.steps)
+    elapsed = time.perf_counter() - t0
+    st.close()
+    value = md.ncells * 4 * args.steps / elapsed / 1e6
+    line = {
+        "impl": "reference", "metric": "Mcell-stage/s", "value": value, "unit": "Mcell-stage/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": name, "cells": md.ncells, "precision": "fp64", "dt": dt},
+        "cpu_baseline": {"value": value, "unit": "Mcell-stage/s", "cores": nthreads, "kind": "port",
+                         "sample": "%d RK4 steps of the full mesh after %d warm-up steps" % (args.steps, args.warmup)},
+        "e2e": {"value": value, "unit": "Mcell-stage/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cfl_dt_host(md, U, cfl):
+    """Host restatement of the device CFL rule (used by the CPU-only arm)."""
+    R, g = 287.05, 1.4
+    r = U[:, 0]
+    u, v, w = U[:, 1] / r, U[:, 2] / r, U[:, 3] / r
+    T = (U[:, 4] / r - 0.5 * (u * u + v * v + w * w)) * (g - 1.0) / R
+    a = np.sqrt(g * R * T)
+    s = np.zeros(md.ncells)
+
+    def add(cells, nrm):
+        nn = np.sqrt((nrm ** 2).sum(1))
+        un = np.abs(u[cells] * nrm[:, 0] + v[cells] * nrm[:, 1] + w[cells] * nrm[:, 2])
+        np.add.at(s, cells, un + a[cells] * nn)
+
+    fi = md.internal
+    add(fi.conn[:, 0], fi.normal)
+    add(fi.conn[:, 1], fi.normal)
+    for b in md.bc:
+        add(b.conn[:, 0], b.normal)
+    return float(cfl * np.min(md.cell_volumes / s))
+
+
+def time_steps(ma, solver, K):
+    import torch
+    stream = torch.cuda.ExternalStream(solver.stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    solver.step(K)
+    e1.record(stream)
+    solver.synchronize()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    import miniaero_gb300 as ma
+    torch.cuda.set_device(local)
+    name = args.workload
+    o = make_options(ma, name, "fp64")
+    md = ma.Parallel3DMesh.from_options(o).fill_mesh_data()
+    U0 = ma.initial_state(md, o)
+    C = md.ncells
+    dmesh = ma.DeviceMesh(md)
+    solver = ma.TimeSolverExplicitRK4(md, o, device_mesh=dmesh)
+    solver.set_state(U0)
+    dt = solver.dt
+    solver.step(args.warmup)
+    solver.synchronize()
+
+    # ---- timed region: K steps from device-resident state ----
+    sampler = ClockSampler(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    sampler.start()
+    ms = time_steps(ma, solver, args.steps)
+    clocks = sampler.stop()
+    barrier(world)
+    ms = allreduce_max(world, ms)
+    launches = solver.launches_per_step * args.steps
+    value = world * C * 4 * args.steps / (ms / 1e3) / 1e6
+    U_fp64 = solver.get_state()
+    steps_fp64 = solver.steps_done
+
+    # ---- per-kernel durations (same workload, kernels launched one by one) ----
+    prof = solver.profile_steps(max(2, min(args.steps, 10)))
+    total_ms = sum(v[0] for v in prof.values())
+    kernels = {k: {"ms_per_launch": v[0] / v[1], "launches": v[1], "share": v[0] / total_ms} for k, v in prof.items()}
+    dom = max(kernels, key=lambda k: kernels[k]["share"])
+    Fi = md.internal.nfaces
+    alg_bytes = FLUX_BYTES_PER_FACE * Fi + FLUX_BYTES_PER_CELL * C
+    peak, peak_kind = load_peaks()
+    flux_ms = kernels["internal_face_flux"]["ms_per_launch"]
+    achieved = alg_bytes / (flux_ms / 1e3) / 1e9
+    roofline = {"kernel": "internal_face_flux", "bound": "hbm", "achieved": achieved, "peak": peak,
+                "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": load_traffic("internal_face_flux"),
+                "algorithmic_bytes_per_launch": alg_bytes, "ms_per_launch": flux_ms,
+                "dominant_kernel": dom}
+
+    # ---- mixed form on the same mesh: throughput and error vs FP64 ----
+    om = make_options(ma, name, "mixed")
+    msolver = ma.TimeSolverExplicitRK4(md, om, device_mesh=dmesh)
+    msolver.set_state(U0)
+    msolver.dt = dt
+    msolver.step(args.warmup)
+    msolver.synchronize()
+    mms = time_steps(ma, msolver, args.steps)
+    mms = allreduce_max(world, mms)
+    mvalue = world * C * 4 * args.steps / (mms / 1e3) / 1e6
+    msolver.set_state(U0)
+    msolver.dt = dt
+    msolver.step(steps_fp64)
+    msolver.synchronize()
+    Um = msolver.get_state()
+    errs = [float(np.linalg.norm(Um[:, k] - U_fp64[:, k]) / max(np.linalg.norm(U_fp64[:, k]), 1e-300))
+            for k in range(5)]
+    mprof = msolver.profile_steps(2)
+    msolver.close()
+
+    # ---- end to end through the C ABI with pinned host buffers ----
+    eo = make_options(ma, name, "fp64")
+    eo.cfl = 0.0
+    eo.dt = dt
+    esolver = ma.TimeSolverExplicitRK4(md, eo, device_mesh=dmesh)
+    hU = torch.empty((C, 5), dtype=torch.float64).pin_memory()
+    hU.numpy()[:] = U0
+    hOut = torch.empty((C, 5), dtype=torch.float64).pin_memory()
+    state_bytes = C * 5 * 8
+    L = ma._lib.lib()
+    inp = ma._lib.f64p(hU.numpy())
+    outp = ma._lib.f64p(hOut.numpy())
+
+    def e2e_step():
+        ma._lib.check(L.ma_solver_set_state(esolver._h, inp, ma.MA_LAYOUT_SOA))
+        ma._lib.check(L.ma_solver_step(esolver._h, 1))
+        ma._lib.check(L.ma_solver_get_state(esolver._h, outp, ma.MA_LAYOUT_SOA))
+
+    for _ in range(max(1, min(args.warmup, 2))):
+        e2e_step()
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = allreduce_max(world, time.perf_counter() - t0)
+    barrier(world)
+    e2e_value = world * C * 4 * args.steps / e2e_s / 1e6
+    esolver.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import oracle
+        cpu = cpu_baseline_sample(ma, oracle, md, o, U0, dt)
+    solver.close()
+
+    if rank == 0:
+        line = {
+            "metric": "Mcell-stage/s", "value": value, "unit": "Mcell-stage/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded mesh generator; Sod initial state)",
+            "config": {"workload": name, "cells": C, "internal_faces": Fi, "precision": "fp64", "dt": dt,
+                       "l2": "working set ~3 GB >> 129 MB L2 (no flush needed)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "clocks": clocks,
+            "e2e": {"value": e2e_value, "unit": "Mcell-stage/s", "h2d_bytes_per_step": state_bytes,
+                    "d2h_bytes_per_step": state_bytes,
+                    "path": "ma_solver_set_state + ma_solver_step + ma_solver_get_state, pinned host SoA buffers"},
+            "gpu_launches": launches,
+            "roofline": roofline,
+            "kernels": kernels,
+            "mixed": {"value": mvalue, "unit": "Mcell-stage/s", "ms_per_step": mms / args.steps,
+                      "speedup_vs_fp64": mvalue / value, "rel_l2_error_vs_fp64": errs,
+                      "error_after_steps": int(steps_fp64),
+                      "kernels": {k: {"ms_per_launch": v[0] / v[1], "launches": v[1]} for k, v in mprof.items()}},
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

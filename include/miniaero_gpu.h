@@ -156,6 +156,16 @@ ma_status ma_solver_get_residual(ma_solver* s, double* res, int32_t layout);
  * on the solver's stream. */
 ma_status ma_solver_step(ma_solver* s, int32_t nsteps);
 ma_status ma_solver_synchronize(ma_solver* s);
+/* Kernel kinds reported by ma_solver_profile_steps. */
+#define MA_PROFILE_KINDS 4
+enum { MA_KERNEL_SWEEP = 0,          /* gradient + min/max + limiter, per cell */
+       MA_KERNEL_INTERNAL_FLUX = 1,  /* Roe + viscous flux, per internal face */
+       MA_KERNEL_BC_FLUX = 2,        /* boundary-face flux */
+       MA_KERNEL_RESIDUAL = 3 };     /* ordered gather + RK4 update, per cell */
+/* Advances nsteps steps like ma_solver_step but launching kernels one by one
+ * with CUDA events around each on the solver's stream; returns the summed
+ * milliseconds and launch counts per kernel kind (arrays of MA_PROFILE_KINDS). */
+ma_status ma_solver_profile_steps(ma_solver* s, int32_t nsteps, double* kernel_ms, int32_t* kernel_launches);
 /* The solver's cudaStream_t, for event timing by the caller. */
 void* ma_solver_stream(ma_solver* s);
 double ma_solver_dt(const ma_solver* s);
@@ -169,6 +179,13 @@ ma_status ma_solver_set_dt(ma_solver* s, double dt);
 ma_status ma_solver_check_state(ma_solver* s, int64_t* bad_cell);
 /* One full solve as the reference's Solve(): init + ntimesteps steps. */
 ma_status ma_solver_solve(ma_solver* s, const ma_host_mesh* host_mesh);
+
+/* ---- diagnostics (host only) -------------------------------------------- */
+/* First n outputs of the glibc rand() sequence for seed (the generator behind
+ * std::random_shuffle in Parallel3DMesh.h:362). */
+ma_status ma_debug_glibc_rand(uint32_t seed, int32_t n, int32_t* out);
+/* Serial Kokkos BinSort permutation of keys (Faces.h:128-144). */
+ma_status ma_debug_binsort(const int32_t* keys, int32_t n, int32_t* perm);
 
 /* ---- operator-level entry points (unit parity; host arrays in and out) --- */
 /* roe_flux::compute_flux (Roe_Flux.h:50) on n independent faces:

@@ -265,6 +265,13 @@ class TimeSolverExplicitRK4:
         self.synchronize()
         return self.get_state()
 
+    def profile_steps(self, nsteps):
+        """Steps with CUDA events around each kernel; {kind: (ms_total, launches)}."""
+        ms = np.zeros(_lib.MA_PROFILE_KINDS, np.float64)
+        n = np.zeros(_lib.MA_PROFILE_KINDS, np.int32)
+        check(lib().ma_solver_profile_steps(self._h, int(nsteps), f64p(ms), i32p(n)))
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(_lib.KERNEL_KINDS) if n[i] > 0}
+
     def check_state(self):
         bad = ctypes.c_int64(-1)
         st = lib().ma_solver_check_state(self._h, ctypes.byref(bad))

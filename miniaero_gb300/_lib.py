@@ -17,6 +17,8 @@ MA_PREC_FP64, MA_PREC_MIXED = 0, 1
 MA_LAYOUT_AOS, MA_LAYOUT_SOA = 0, 1
 MA_IC_REFERENCE, MA_IC_SOD, MA_IC_CONSTANT = 0, 1, 2
 MA_MAX_BC_SETS = 16
+MA_PROFILE_KINDS = 4
+KERNEL_KINDS = ("sweep_gradient_limiter", "internal_face_flux", "boundary_face_flux", "residual_rk_update")
 
 c_int32 = ctypes.c_int32
 c_double = ctypes.c_double
@@ -111,6 +113,7 @@ _SIGNATURES = {
     "ma_solver_get_residual": (c_int32, [c_void_p, P_f64, c_int32]),
     "ma_solver_step": (c_int32, [c_void_p, c_int32]),
     "ma_solver_synchronize": (c_int32, [c_void_p]),
+    "ma_solver_profile_steps": (c_int32, [c_void_p, c_int32, P_f64, P_i32]),
     "ma_solver_stream": (c_void_p, [c_void_p]),
     "ma_solver_dt": (c_double, [c_void_p]),
     "ma_solver_steps_done": (ctypes.c_int64, [c_void_p]),
@@ -118,6 +121,8 @@ _SIGNATURES = {
     "ma_solver_set_dt": (c_int32, [c_void_p, c_double]),
     "ma_solver_check_state": (c_int32, [c_void_p, ctypes.POINTER(ctypes.c_int64)]),
     "ma_solver_solve": (c_int32, [c_void_p, c_void_p]),
+    "ma_debug_glibc_rand": (c_int32, [ctypes.c_uint32, c_int32, P_i32]),
+    "ma_debug_binsort": (c_int32, [P_i32, c_int32, P_i32]),
     "ma_op_roe_flux": (c_int32, [c_int32, P_f64, P_f64, P_f64, P_f64, P_f64, P_f64]),
     "ma_op_viscous_flux": (c_int32, [c_int32, P_f64, P_f64, P_f64, c_int32, c_double, c_double, P_f64]),
     "ma_op_limiter": (c_int32, [c_int32, c_int32, P_f64, P_f64, P_f64, P_f64, P_f64]),

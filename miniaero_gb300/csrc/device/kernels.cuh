@@ -65,13 +65,18 @@ struct PathConfig {
 // Launch counts per RK stage for the given configuration.
 int launches_per_stage(const PathConfig& cfg, const TopoView& t);
 
+// Kernel selection bits for launch_stage (profiling launches one at a time).
+enum KernelBits : unsigned {
+  kSweep1 = 1u, kInternalFlux = 2u, kBcFlux = 4u, kResidual = 8u, kAllKernels = 15u
+};
+
 template <class R>
 cudaError_t launch_init_primitives(const TopoView& t, const StateBuffers& s, const StageBuffers<R>& b,
                                    cudaStream_t stream);
 
 template <class R>
 cudaError_t launch_stage(const TopoView& t, const GeomView<R>& g, const PathConfig& cfg, const StateBuffers& s,
-                         const StageBuffers<R>& b, int stage, cudaStream_t stream);
+                         const StageBuffers<R>& b, int stage, cudaStream_t stream, unsigned kernels = kAllKernels);
 
 // Defined in kernels_fp64.cu (plain form) and kernels_mixed.cu (mixed form).
 template <>
@@ -82,10 +87,10 @@ cudaError_t launch_init_primitives<float>(const TopoView&, const StateBuffers&, 
                                           cudaStream_t);
 template <>
 cudaError_t launch_stage<double>(const TopoView&, const GeomView<double>&, const PathConfig&, const StateBuffers&,
-                                 const StageBuffers<double>&, int, cudaStream_t);
+                                 const StageBuffers<double>&, int, cudaStream_t, unsigned);
 template <>
 cudaError_t launch_stage<float>(const TopoView&, const GeomView<float>&, const PathConfig&, const StateBuffers&,
-                                const StageBuffers<float>&, int, cudaStream_t);
+                                const StageBuffers<float>&, int, cudaStream_t, unsigned);
 
 // Operator-level kernels (unit parity, FP64).
 cudaError_t launch_op_roe(int n, const double* pl, const double* pr, const double* normal, const double* tangent,

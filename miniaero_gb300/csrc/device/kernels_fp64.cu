@@ -14,8 +14,8 @@ cudaError_t launch_init_primitives<double>(const TopoView& t, const StateBuffers
 template <>
 cudaError_t launch_stage<double>(const TopoView& t, const GeomView<double>& g, const PathConfig& cfg,
                                  const StateBuffers& s, const StageBuffers<double>& b, int stage,
-                                 cudaStream_t stream) {
-  return launch_stage_impl<double>(t, g, cfg, s, b, stage, stream);
+                                 cudaStream_t stream, unsigned kernels) {
+  return launch_stage_impl<double>(t, g, cfg, s, b, stage, stream, kernels);
 }
 
 }  // namespace dev

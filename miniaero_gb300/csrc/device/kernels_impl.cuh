@@ -340,10 +340,11 @@ cudaError_t launch_init_primitives_impl(const TopoView& t, const StateBuffers& s
 
 template <class R>
 cudaError_t launch_stage_impl(const TopoView& t, const GeomView<R>& g, const PathConfig& cfg, const StateBuffers& s,
-                              const StageBuffers<R>& b, int stage, cudaStream_t stream) {
+                              const StageBuffers<R>& b, int stage, cudaStream_t stream, unsigned kernels) {
   if (t.C == 0) return cudaSuccess;
   const unsigned gc = blocks_for(t.C, kCellBlock);
-  if (cfg.second_order) {
+  if (!(kernels & kSweep1)) {
+  } else if (cfg.second_order) {
     if (cfg.limiter == 1)
       k_sweep1<R, 2><<<gc, kCellBlock, 0, stream>>>(t, g, b.W, b.grad, b.phi);
     else
@@ -351,7 +352,7 @@ cudaError_t launch_stage_impl(const TopoView& t, const GeomView<R>& g, const Pat
   } else if (cfg.viscous) {
     k_sweep1<R, 0><<<gc, kCellBlock, 0, stream>>>(t, g, b.W, b.grad, b.phi);
   }
-  if (t.Fi > 0) {
+  if (t.Fi > 0 && (kernels & kInternalFlux)) {
     const unsigned gf = blocks_for(t.Fi, kFaceBlock);
     if (cfg.second_order) {
       if (cfg.viscous)
@@ -365,12 +366,13 @@ cudaError_t launch_stage_impl(const TopoView& t, const GeomView<R>& g, const Pat
         k_internal_flux<R, false, false><<<gf, kFaceBlock, 0, stream>>>(t, g, b.W, b.grad, b.phi, cfg.transport, b.fflux);
     }
   }
-  if (t.Fb > 0) {
+  if (t.Fb > 0 && (kernels & kBcFlux)) {
     InflowState inflow;
     for (int k = 0; k < 5; ++k) inflow.u[k] = cfg.inflow[k];
     k_bc_flux<R><<<blocks_for(t.Fb, kFaceBlock), kFaceBlock, 0, stream>>>(t, g, b.W, cfg.transport, inflow, b.fflux);
   }
-  k_residual<R><<<gc, kCellBlock, 0, stream>>>(t, b.fflux, s.Un, s.Unp1, b.W, s.res, cfg.dt, stage);
+  if (kernels & kResidual)
+    k_residual<R><<<gc, kCellBlock, 0, stream>>>(t, b.fflux, s.Un, s.Unp1, b.W, s.res, cfg.dt, stage);
   return cudaGetLastError();
 }
 

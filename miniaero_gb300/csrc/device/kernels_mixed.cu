@@ -14,8 +14,8 @@ cudaError_t launch_init_primitives<float>(const TopoView& t, const StateBuffers&
 template <>
 cudaError_t launch_stage<float>(const TopoView& t, const GeomView<float>& g, const PathConfig& cfg,
                                 const StateBuffers& s, const StageBuffers<float>& b, int stage,
-                                cudaStream_t stream) {
-  return launch_stage_impl<float>(t, g, cfg, s, b, stage, stream);
+                                cudaStream_t stream, unsigned kernels) {
+  return launch_stage_impl<float>(t, g, cfg, s, b, stage, stream, kernels);
 }
 
 }  // namespace dev

@@ -546,6 +546,54 @@ extern "C" ma_status ma_solver_step(ma_solver* s, int32_t nsteps) {
   return MA_OK;
 }
 
+extern "C" ma_status ma_solver_profile_steps(ma_solver* s, int32_t nsteps, double* kernel_ms, int32_t* kernel_launches) {
+  if (!s || nsteps < 0 || !kernel_ms || !kernel_launches) return set_error(MA_EINVAL, "ma_solver_profile_steps: bad arguments");
+  if (!s->state_set) return set_error(MA_ESTATE, "solver state has not been set");
+  MA_CUDA_TRY(cudaSetDevice(s->mesh->device));
+  for (int k = 0; k < MA_PROFILE_KINDS; ++k) { kernel_ms[k] = 0.0; kernel_launches[k] = 0; }
+  const dev::TopoView& t = s->mesh->topo;
+  const unsigned bits[MA_PROFILE_KINDS] = {dev::kSweep1, dev::kInternalFlux, dev::kBcFlux, dev::kResidual};
+  bool present[MA_PROFILE_KINDS] = {s->cfg.second_order || s->cfg.viscous, t.Fi > 0, t.Fb > 0, true};
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> kind;
+  auto cleanup = [&]() { for (cudaEvent_t e : ev) cudaEventDestroy(e); };
+  for (int32_t step = 0; step < nsteps; ++step)
+    for (int stage = 0; stage < 4; ++stage)
+      for (int k = 0; k < MA_PROFILE_KINDS; ++k) {
+        if (!present[k]) continue;
+        cudaEvent_t a, b;
+        if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+          cleanup();
+          return set_error(MA_ECUDA, "ma_solver_profile_steps: cudaEventCreate failed");
+        }
+        ev.push_back(a);
+        ev.push_back(b);
+        kind.push_back(k);
+        cudaEventRecord(a, s->stream);
+        cudaError_t e = s->mixed ? dev::launch_stage<float>(t, s->mesh->g32, s->cfg, s->st, s->b32, stage, s->stream, bits[k])
+                                 : dev::launch_stage<double>(t, s->mesh->g64, s->cfg, s->st, s->b64, stage, s->stream, bits[k]);
+        cudaEventRecord(b, s->stream);
+        if (e != cudaSuccess) {
+          cleanup();
+          return set_error(MA_ECUDA, std::string("ma_solver_profile_steps: ") + cudaGetErrorString(e));
+        }
+      }
+  cudaError_t e = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess) {
+    cleanup();
+    return set_error(MA_ECUDA, std::string("ma_solver_profile_steps: ") + cudaGetErrorString(e));
+  }
+  for (size_t i = 0; i < kind.size(); ++i) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev[2 * i], ev[2 * i + 1]);
+    kernel_ms[kind[i]] += ms;
+    kernel_launches[kind[i]] += 1;
+  }
+  cleanup();
+  s->steps_done += nsteps;
+  return MA_OK;
+}
+
 extern "C" ma_status ma_solver_synchronize(ma_solver* s) {
   if (!s) return set_error(MA_EINVAL, "ma_solver_synchronize: null solver");
   MA_CUDA_TRY(cudaStreamSynchronize(s->stream));

@@ -2,6 +2,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "../../../include/miniaero_gpu.h"
 #include "errors.hpp"
@@ -90,6 +91,20 @@ extern "C" ma_status ma_host_mesh_view(const ma_host_mesh* m, ma_mesh_view* v) {
 }
 
 extern "C" void ma_host_mesh_free(ma_host_mesh* m) { delete m; }
+
+extern "C" ma_status ma_debug_glibc_rand(uint32_t seed, int32_t n, int32_t* out) {
+  if (n < 0 || (n > 0 && !out)) return set_error(MA_EINVAL, "ma_debug_glibc_rand: bad arguments");
+  miniaero::GlibcRand r(seed);
+  for (int32_t i = 0; i < n; ++i) out[i] = r.next();
+  return MA_OK;
+}
+
+extern "C" ma_status ma_debug_binsort(const int32_t* keys, int32_t n, int32_t* perm) {
+  if (n < 0 || (n > 0 && (!keys || !perm))) return set_error(MA_EINVAL, "ma_debug_binsort: bad arguments");
+  const std::vector<int32_t> p = miniaero::binsort_permutation(keys, n, 1);
+  for (int32_t i = 0; i < n; ++i) perm[i] = p[i];
+  return MA_OK;
+}
 
 // Initial conditions (kokkos/Initial_Conditions.h:38-133).
 extern "C" ma_status ma_host_initial_state(const ma_host_mesh* hm, const ma_options* o, double* U) {

@@ -52,6 +52,11 @@ def lib():
         L.oracle_vanalbada.restype = ctypes.c_double
         L.oracle_vanalbada.argtypes = [ctypes.c_double] * 3
         L.oracle_primitives.argtypes = [P_f64, P_f64]
+        L.oracle_create.restype = ctypes.c_void_p
+        L.oracle_create.argtypes = [ctypes.POINTER(oracle_mesh), ctypes.POINTER(oracle_options), P_f64, ctypes.c_int]
+        L.oracle_step.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.oracle_get_state.argtypes = [ctypes.c_void_p, P_f64, P_f64]
+        L.oracle_free.argtypes = [ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -91,13 +96,7 @@ class OracleMesh:
         self.c = m
 
 
-def solve(md, options, U0, nsteps=None, dt=None, nthreads=1, return_residual=False):
-    """Advances U0 ((ncells, 5) conserved) with the reference semantics.
-
-    options: a miniaero_gb300.Options (second_order_space, viscous, limiter,
-    viscosity_model, mu, prandtl, dt, ntimesteps, inflow_state).
-    """
-    om = OracleMesh(md)
+def _c_options(options, nsteps=None, dt=None):
     o = oracle_options()
     o.second_order = int(options.second_order_space)
     o.viscous = int(options.viscous)
@@ -109,6 +108,46 @@ def solve(md, options, U0, nsteps=None, dt=None, nthreads=1, return_residual=Fal
     o.nsteps = int(options.ntimesteps if nsteps is None else nsteps)
     for k in range(5):
         o.inflow_state[k] = options.inflow_state[k]
+    return o
+
+
+class Stepper:
+    """Persistent oracle state advanced step by step (CPU baseline timing)."""
+
+    def __init__(self, md, options, U0, dt=None, nthreads=1):
+        self.mesh = OracleMesh(md)
+        self.opts = _c_options(options, 0, dt)
+        self.ncells = md.ncells
+        U0 = np.ascontiguousarray(U0, dtype=np.float64)
+        self.h = lib().oracle_create(ctypes.byref(self.mesh.c), ctypes.byref(self.opts), _p(U0, P_f64), int(nthreads))
+        if not self.h:
+            raise RuntimeError("oracle_create failed")
+
+    def step(self, n=1):
+        lib().oracle_step(self.h, int(n))
+
+    def state(self):
+        U = np.empty((self.ncells, 5))
+        lib().oracle_get_state(self.h, _p(U, P_f64), ctypes.cast(None, P_f64))
+        return U
+
+    def close(self):
+        if self.h:
+            lib().oracle_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+def solve(md, options, U0, nsteps=None, dt=None, nthreads=1, return_residual=False):
+    """Advances U0 ((ncells, 5) conserved) with the reference semantics.
+
+    options: a miniaero_gb300.Options (second_order_space, viscous, limiter,
+    viscosity_model, mu, prandtl, dt, ntimesteps, inflow_state).
+    """
+    om = OracleMesh(md)
+    o = _c_options(options, nsteps, dt)
     U = np.ascontiguousarray(U0, dtype=np.float64).copy()
     res = np.zeros_like(U) if return_residual else None
     rc = lib().oracle_solve(ctypes.byref(om.c), ctypes.byref(o), _p(U, P_f64),

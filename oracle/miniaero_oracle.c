@@ -559,37 +559,52 @@ static void apply_cell_flux(ostate* s) {
     }
 }
 
-int oracle_solve(const oracle_mesh* m, const oracle_options* o, double* U, double* res_out, int nthreads) {
-  if (!m || !o || !U || m->ncells <= 0) return 1;
-  const int C = m->ncells;
-  ostate st;
-  ostate* s = &st;
-  memset(s, 0, sizeof(*s));
+struct oracle_state {
+  ostate s;
+  double* pool;
+  double* Un;
+};
+
+oracle_state* oracle_create(const oracle_mesh* m, const oracle_options* o, const double* U0, int nthreads) {
+  if (!m || !o || !U0 || m->ncells <= 0) return NULL;
+  const size_t C = (size_t)m->ncells;
+  oracle_state* h = (oracle_state*)calloc(1, sizeof(oracle_state));
+  if (!h) return NULL;
+  h->pool = (double*)calloc(C * (5 * 10 + 15 * 2), sizeof(double));
+  if (!h->pool) { free(h); return NULL; }
+  ostate* s = &h->s;
   s->m = m;
   s->o = o;
   s->nt = nthreads > 0 ? nthreads : 1;
   s->par = s->nt > 1;
-  double* pool = (double*)calloc((size_t)C * (5 * 9 + 15 * 2), sizeof(double));
-  if (!pool) return 2;
-  double* q = pool;
-  s->Un = U;
-  s->Unp1 = q; q += 5 * (size_t)C;
-  s->Utmp = q; q += 5 * (size_t)C;
-  s->res = q; q += 5 * (size_t)C;
-  s->cell_flux = q; q += 5 * (size_t)C;
-  s->smin = q; q += 5 * (size_t)C;
-  s->smax = q; q += 5 * (size_t)C;
-  s->slim = q; q += 5 * (size_t)C;
-  s->lim = q; q += 5 * (size_t)C;
-  q += 5 * (size_t)C;
-  s->cell_grad = q; q += 15 * (size_t)C;
-  s->grad = q; q += 15 * (size_t)C;
+  double* q = h->pool;
+  h->Un = q; q += 5 * C;
+  s->Un = h->Un;
+  s->Unp1 = q; q += 5 * C;
+  s->Utmp = q; q += 5 * C;
+  s->res = q; q += 5 * C;
+  s->cell_flux = q; q += 5 * C;
+  s->smin = q; q += 5 * C;
+  s->smax = q; q += 5 * C;
+  s->slim = q; q += 5 * C;
+  s->lim = q; q += 5 * C;
+  q += 5 * C;
+  s->cell_grad = q; q += 15 * C;
+  s->grad = q; q += 15 * C;
+  memcpy(s->Un, U0, sizeof(double) * 5 * C);
+  memcpy(s->Unp1, s->Un, sizeof(double) * 5 * C);    /* copy (TimeSolverExplicitRK4.h:335) */
+  return h;
+}
 
+void oracle_step(oracle_state* h, int nsteps) {
   static const double alpha[4] = {0.0, 1.0 / 2.0, 1.0 / 2.0, 1.0};
   static const double beta[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
-
-  memcpy(s->Unp1, s->Un, sizeof(double) * 5 * (size_t)C);    /* copy (TimeSolverExplicitRK4.h:335) */
-  for (int step = 1; step <= o->nsteps; ++step) {               /* Solve loop, :340-491 */
+  static const int type_order[4] = {0, 1, 3, 2};  /* Extrapolate, Tangent, NoSlip, Inflow */
+  ostate* s = &h->s;
+  const oracle_mesh* m = s->m;
+  const oracle_options* o = s->o;
+  const size_t C = (size_t)m->ncells;
+  for (int step = 1; step <= nsteps; ++step) {                 /* Solve loop, :340-491 */
     for (int irk = 0; irk < 4; ++irk) {
       update(s, alpha[irk], s->res, s->Un, s->Utmp);
       zero_cell_flux(s);
@@ -599,18 +614,34 @@ int oracle_solve(const oracle_mesh* m, const oracle_options* o, double* U, doubl
         limiter(s);
       }
       internal_flux(s);
-      for (int t = 0; t < 4; ++t) {                             /* BC types: Extrapolate, Tangent, NoSlip, Inflow */
-        static const int type_order[4] = {0, 1, 3, 2};
+      for (int t = 0; t < 4; ++t)
         for (int b = 0; b < m->nbc; ++b)
           if (m->bc[b].type == type_order[t]) bc_flux(s, &m->bc[b]);
-      }
       apply_cell_flux(s);
       update(s, beta[irk], s->res, s->Unp1, s->Unp1);
     }
-    memcpy(s->Un, s->Unp1, sizeof(double) * 5 * (size_t)C);
+    memcpy(s->Un, s->Unp1, sizeof(double) * 5 * C);
   }
-  if (res_out) memcpy(res_out, s->res, sizeof(double) * 5 * (size_t)C);
-  free(pool);
+}
+
+void oracle_get_state(const oracle_state* h, double* U, double* res) {
+  const size_t C = (size_t)h->s.m->ncells;
+  if (U) memcpy(U, h->s.Un, sizeof(double) * 5 * C);
+  if (res) memcpy(res, h->s.res, sizeof(double) * 5 * C);
+}
+
+void oracle_free(oracle_state* h) {
+  if (!h) return;
+  free(h->pool);
+  free(h);
+}
+
+int oracle_solve(const oracle_mesh* m, const oracle_options* o, double* U, double* res_out, int nthreads) {
+  oracle_state* h = oracle_create(m, o, U, nthreads);
+  if (!h) return 1;
+  oracle_step(h, o->nsteps);
+  oracle_get_state(h, U, res_out);
+  oracle_free(h);
   return 0;
 }
 

@@ -59,6 +59,14 @@ typedef struct {
 int oracle_solve(const oracle_mesh* mesh, const oracle_options* opts, double* U, double* res_out,
                  int nthreads);
 
+/* Persistent solver state for step-by-step use (timing). The mesh and options
+ * must outlive the state. */
+typedef struct oracle_state oracle_state;
+oracle_state* oracle_create(const oracle_mesh* mesh, const oracle_options* opts, const double* U0, int nthreads);
+void oracle_step(oracle_state* h, int nsteps);
+void oracle_get_state(const oracle_state* h, double* U, double* res);
+void oracle_free(oracle_state* h);
+
 /* Reference Sod initial condition (Initial_Conditions.h:38-96) on U[ncells*5]. */
 void oracle_init_sod_reference(const oracle_mesh* mesh, double midx, double* U);
 

@@ -1,0 +1,83 @@
+"""The oracle (and the host mesh it runs on) against the reference's own
+golden vectors: kokkos/tests/{3D_Sod,Ramp,FlatPlate}_Serial/results.gold,
+compared with the reference's numeric_text_diff rule and tolerances
+(3d_sod_serial_test.sh:4, ramp_serial_test.sh:4, flatplate_serial_test.sh:4).
+Runs where the reference tree is present (CPU container)."""
+import os
+
+import numpy as np
+import pytest
+
+import miniaero_gb300 as ma
+import oracle
+from tests.numeric_text_diff import compare_lines
+
+CASES = [("3D_Sod_Serial", 1e-3, 1e-6), ("Ramp_Serial", 1e-2, 1e-3), ("FlatPlate_Serial", 1e-2, 1e-3)]
+
+
+def results_lines(md, U):
+    """results.<rank> text as TimeSolverExplicitRK4.h:527-536 writes it (%g fields, tab separated)."""
+    lines = []
+    for c in range(md.ncells):
+        x = md.cell_coords[c]
+        lines.append("".join("%g\t" % v for v in (x[0], x[1], x[2], *U[c])))
+    return lines
+
+
+@pytest.mark.parametrize("case,rel,floor", CASES)
+def test_oracle_matches_reference_gold(reference_dir, case, rel, floor):
+    o = ma.Options.read_options_file(os.path.join(reference_dir, "tests", case, "miniaero.inp"))
+    md = ma.Parallel3DMesh.from_options(o).fill_mesh_data()
+    U = oracle.solve(md, o, ma.initial_state(md, o))
+    with open(os.path.join(reference_dir, "tests", case, "results.gold")) as f:
+        gold = f.read().splitlines()
+    mine = results_lines(md, U)
+    assert compare_lines(mine, gold, rel, floor) == []
+    # Stronger than the reference rule: every field above 1e-3 in magnitude is
+    # textually identical at the 6 printed digits.
+    bad = 0
+    for a, b in zip(mine, gold):
+        for x, y in zip(a.split(), b.split()):
+            if x != y and max(abs(float(x)), abs(float(y))) > 1e-3:
+                bad += 1
+    assert bad == 0
+
+
+def test_oracle_threads_agree_with_serial():
+    """The OpenMP oracle (timing baseline) sums in another order: equal to round-off."""
+    o = ma.Options(problem_type=1, lx=2.0, ly=0.002, lz=1.0, nx=16, ny=16, nz=2, ntimesteps=20, dt=3e-8,
+                   second_order_space=1, viscous=1)
+    md = ma.Parallel3DMesh.from_options(o).fill_mesh_data()
+    U0 = ma.initial_state(md, o)
+    a = oracle.solve(md, o, U0, nthreads=1)
+    b = oracle.solve(md, o, U0, nthreads=4)
+    # momentum components share one scale (the transverse ones are round-off sized)
+    scale = np.abs(a).max(axis=0)
+    scale[1:4] = scale[1:4].max()
+    assert np.max(np.abs(a - b) / scale) < 1e-12
+
+
+def test_oracle_conserves_mass_with_closed_walls():
+    """Tangent walls on every side: total mass is constant to round-off."""
+    o = ma.Options(problem_type=0, lx=1.0, ly=0.5, lz=0.5, nx=12, ny=6, nz=6, ntimesteps=10, dt=1e-5,
+                   second_order_space=1, viscous=1, ic=ma.MA_IC_SOD, viscosity_model=ma.MA_VISC_CONSTANT,
+                   mu=1.8e-5, prandtl=0.72, bc_override=[1, 1, 1, 1, 1, 1])
+    md = ma.Parallel3DMesh.from_options(o).fill_mesh_data()
+    U0 = ma.initial_state(md, o)
+    U = oracle.solve(md, o, U0)
+    m0 = float((U0[:, 0] * md.cell_volumes).sum())
+    m1 = float((U[:, 0] * md.cell_volumes).sum())
+    assert abs(m1 - m0) / m0 < 1e-13
+    assert not np.allclose(U, U0)
+
+
+def test_oracle_preserves_uniform_flow():
+    """A uniform state with inflow equal to it and extrapolation elsewhere stays uniform."""
+    o = ma.Options(problem_type=2, lx=1.0, ly=1.0, lz=0.5, nx=8, ny=8, nz=2, ntimesteps=5, dt=1e-6,
+                   second_order_space=1, viscous=0, bc_override=[0, 0, 0, 0, 0, 2])
+    md = ma.Parallel3DMesh.from_options(o).fill_mesh_data()
+    U0 = ma.initial_state(md, o)
+    U = oracle.solve(md, o, U0)
+    scale = np.abs(U0).max(axis=0)
+    scale[1:4] = scale[1:4].max()
+    assert np.max(np.abs(U - U0) / scale) < 1e-12

@@ -187,6 +187,12 @@ ma_status ma_debug_glibc_rand(uint32_t seed, int32_t n, int32_t* out);
 /* Serial Kokkos BinSort permutation of keys (Faces.h:128-144). */
 ma_status ma_debug_binsort(const int32_t* keys, int32_t n, int32_t* perm);
 
+/* Checks the device's reciprocal-based correctly rounded division against
+ * IEEE division on n generated pairs (mode 0 random, 1 divisors with an
+ * all-ones significand, 2 quotients near rounding midpoints). Returns the
+ * mismatch count and, if any, one failing pair in example[0..1]. */
+ma_status ma_debug_check_division(int32_t mode, uint64_t n, uint64_t seed, uint64_t* mismatches, double* example);
+
 /* ---- operator-level entry points (unit parity; host arrays in and out) --- */
 /* roe_flux::compute_flux (Roe_Flux.h:50) on n independent faces:
  * pl, pr [n*5] primitives; normal, tangent, binormal [n*3]; flux [n*5]. */

@@ -17,6 +17,7 @@ struct TopoView {
   int32_t C = 0, Fi = 0, Fb = 0, F = 0;
   int32_t nbc_type[4] = {0, 0, 0, 0};  // BC face counts in type order E, T, N, I
   const double* vol = nullptr;         // [C]
+  const double* vinv = nullptr;        // [C] 1/V rounded to nearest
   const int32_t* fconn = nullptr;      // [2][F] (left, right); right = -1 on a boundary
   // Per-cell contribution lists, slot-major [kMaxCellFaces][C], code =
   // (face << 1) | (cell is the face's left cell), -1 for an unused slot.
@@ -29,6 +30,7 @@ struct TopoView {
 template <class R>
 struct GeomView {
   const R* vol = nullptr;  // [C]
+  const R* vinv = nullptr; // [C] 1/V rounded to nearest
   const R* fn = nullptr;   // [3][F] area vector
   const R* fnu = nullptr;  // [3][F] unit normal
   const R* ftu = nullptr;  // [3][F] unit tangent
@@ -53,11 +55,28 @@ struct StateBuffers {
   double* res = nullptr;   // [5][C] optional
 };
 
+// Conserved inflow state passed by value to the boundary kernels.
+struct InflowState {
+  double u[5];
+};
+
+// One mesh instance of a batch: its mesh views, work arrays, state, time step
+// and inflow state.
+template <class R>
+struct Segment {
+  TopoView t;
+  GeomView<R> g;
+  StageBuffers<R> b;
+  StateBuffers s;
+  double dt;
+  InflowState inflow;
+};
+
 struct PathConfig {
   bool second_order = false;
   bool viscous = false;
   int limiter = 0;  // 0 Venkatakrishnan, 1 Van Albada
-  Transport transport{0, 0.0, 0.0};
+  Transport transport{0, 0.0, 0.0, 0.0};
   double inflow[5] = {0, 0, 0, 0, 0};
   double dt = 0.0;
 };
@@ -100,6 +119,10 @@ cudaError_t launch_op_viscous(int n, const double* grad, const double* prim, con
 cudaError_t launch_op_limiter(int n, int kind, const double* dumax, const double* dumin, const double* du,
                               const double* d2, double* phi, cudaStream_t stream);
 cudaError_t launch_op_primitives(int n, const double* U, double* V, cudaStream_t stream);
+
+// div_by_recip against IEEE division on n generated operand pairs.
+cudaError_t launch_check_division(int mode, unsigned long long n, unsigned long long seed,
+                                  unsigned long long* mismatches, double* example, cudaStream_t stream);
 
 // State check: first cell with a non-finite value or non-positive rho / rhoE.
 cudaError_t launch_check_state(int C, const double* Un, unsigned long long* first_bad, cudaStream_t stream);

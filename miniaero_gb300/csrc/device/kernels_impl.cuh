@@ -17,6 +17,7 @@
 #pragma once
 #include <cfloat>
 #include <cstdint>
+#include <type_traits>
 
 #include "kernels.cuh"
 
@@ -28,10 +29,28 @@ namespace {
 constexpr int kCellBlock = 256;
 constexpr int kFaceBlock = 128;
 
-// Conserved inflow state passed by value to the boundary kernel.
-struct InflowState {
-  double u[5];
-};
+// Primitives of an FP64 state written as R: FP64 arithmetic for the plain
+// form (bit-exact), FP32 for the mixed form (its flux work is FP32 anyway).
+template <class R>
+__device__ __forceinline__ void store_primitives(const double ut[5], R* __restrict__ W, int C, int c) {
+  if constexpr (std::is_same<R, double>::value) {
+    double v[5];
+    primitives(ut, v);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) W[k * C + c] = v[k];
+  } else {
+    const float r = static_cast<float>(ut[0]);
+    const float ri = 1.0f / r;
+    const float u = static_cast<float>(ut[1]) * ri, v = static_cast<float>(ut[2]) * ri,
+                w = static_cast<float>(ut[3]) * ri;
+    const float e = static_cast<float>(ut[4]) * ri - 0.5f * (u * u + v * v + w * w);
+    W[c] = r;
+    W[C + c] = u;
+    W[2 * C + c] = v;
+    W[3 * C + c] = w;
+    W[4 * C + c] = e * (0.4f / 287.05f);
+  }
+}
 
 template <class R> __device__ __forceinline__ R big_value();
 template <> __device__ __forceinline__ double big_value<double>() { return 1.0e300; }
@@ -53,15 +72,14 @@ __device__ __forceinline__ FaceFrame<R> load_frame(const GeomView<R>& g, int f, 
 
 // MODE: 0 gradient only (viscous first order), 1 + Venkatakrishnan, 2 + Van Albada.
 template <class R, int MODE>
-__global__ void __launch_bounds__(kCellBlock) k_sweep1(TopoView t, GeomView<R> g, const R* __restrict__ W,
-                                                       R* __restrict__ grad, R* __restrict__ phi) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= t.C) return;
+__device__ __forceinline__ void sweep1_cell(const TopoView& t, const GeomView<R>& g, const R* __restrict__ W,
+                                            R* __restrict__ grad, R* __restrict__ phi, int c) {
   const int C = t.C, F = t.F;
   R wc[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k) wc[k] = W[k * C + c];
   const R V = g.vol[c];
+  const R Vinv = g.vinv[c];  // RN(1/V), see div_by_recip
   R acc[5][3];
   R mn[5], mx[5];
 #pragma unroll
@@ -92,7 +110,7 @@ __global__ void __launch_bounds__(kCellBlock) k_sweep1(TopoView t, GeomView<R> g
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
           const R gr = h * n[d];
-          acc[k][d] += left ? gr / V : -gr / V;
+          acc[k][d] += left ? div_by_recip(gr, V, Vinv) : div_by_recip(-gr, V, Vinv);
         }
         if (MODE > 0) {
           const R fmin_ = (pr < pl) ? pr : pl;
@@ -105,7 +123,7 @@ __global__ void __launch_bounds__(kCellBlock) k_sweep1(TopoView t, GeomView<R> g
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
 #pragma unroll
-        for (int d = 0; d < 3; ++d) acc[k][d] += wc[k] * n[d] / V;
+        for (int d = 0; d < 3; ++d) acc[k][d] += div_by_recip(wc[k] * n[d], V, Vinv);
         if (MODE > 0) {
           mn[k] = (wc[k] < mn[k]) ? wc[k] : mn[k];
           mx[k] = (mx[k] < wc[k]) ? wc[k] : mx[k];
@@ -121,7 +139,39 @@ __global__ void __launch_bounds__(kCellBlock) k_sweep1(TopoView t, GeomView<R> g
       gsum[k][d] = R(0) + acc[k][d];  // green_gauss_gradient_sum
       grad[(3 * k + d) * C + c] = gsum[k][d];
     }
-  if constexpr (MODE > 0) {
+  if constexpr (MODE == 1 && std::is_same<R, double>::value) {
+    // Venkatakrishnan limiter of the cell: min(1, phi_f over its faces) with
+    // phi_f = RN(n_f / d_f). Rounding is monotone, so the minimum equals
+    // RN(min_f n_f / d_f): the smallest ratio is found with exact
+    // cross-multiplied comparisons and divided once per component.
+    R nm[5], dm[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) { nm[k] = 1.0; dm[k] = 1.0; }
+#pragma unroll 1
+    for (int s = 0; s < kMaxCellFaces; ++s) {
+      const int code = t.csr_grad[s * C + c];
+      if (code < 0) continue;
+      const int f = code >> 1;
+      const R* dv = (code & 1) ? g.dL : g.dR;
+      const R disp[3] = {dv[f], dv[F + f], dv[2 * F + f]};
+      R dist = 0;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) dist += disp[d] * disp[d];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        R du = 0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) du += disp[d] * gsum[k][d];
+        R n, dd;
+        if (venkat_ratio(mx[k] - wc[k], mn[k] - wc[k], du, dist, n, dd) && ratio_less(n, dd, nm[k], dm[k])) {
+          nm[k] = n;
+          dm[k] = dd;
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 5; ++k) phi[k * C + c] = (nm[k] == 1.0 && dm[k] == 1.0) ? 1.0 : nm[k] / dm[k];
+  } else if constexpr (MODE > 0) {
     // Limiter: minimum over this cell's faces of the limiter function.
     R lim[5];
 #pragma unroll
@@ -153,11 +203,9 @@ __global__ void __launch_bounds__(kCellBlock) k_sweep1(TopoView t, GeomView<R> g
 }
 
 template <class R, bool SECOND, bool VISC>
-__global__ void __launch_bounds__(kFaceBlock) k_internal_flux(TopoView t, GeomView<R> g, const R* __restrict__ W,
-                                                              const R* __restrict__ grad, const R* __restrict__ phi,
-                                                              Transport tr, R* __restrict__ fflux) {
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= t.Fi) return;
+__device__ __forceinline__ void internal_flux_face(const TopoView& t, const GeomView<R>& g, const R* __restrict__ W,
+                                                   const R* __restrict__ grad, const R* __restrict__ phi,
+                                                   const Transport& tr, R* __restrict__ fflux, int f) {
   const int C = t.C, F = t.F;
   const int L = t.fconn[f];
   const int Rc = t.fconn[F + f];
@@ -203,11 +251,9 @@ __global__ void __launch_bounds__(kFaceBlock) k_internal_flux(TopoView t, GeomVi
 
 // Boundary faces; each writes the contribution its cell adds to the residual.
 template <class R>
-__global__ void __launch_bounds__(kFaceBlock) k_bc_flux(TopoView t, GeomView<R> g, const R* __restrict__ W,
-                                                        Transport tr, InflowState inflow,
-                                                        R* __restrict__ fflux) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= t.Fb) return;
+__device__ __forceinline__ void bc_flux_face(const TopoView& t, const GeomView<R>& g, const R* __restrict__ W,
+                                             const Transport& tr, const InflowState& inflow, R* __restrict__ fflux,
+                                             int i) {
   const int C = t.C, F = t.F;
   const int f = t.Fi + i;
   const int c = t.fconn[f];
@@ -259,12 +305,9 @@ __global__ void __launch_bounds__(kFaceBlock) k_bc_flux(TopoView t, GeomView<R> 
 
 // Ordered residual gather + RK4 update + primitives of the next stage state.
 template <class R>
-__global__ void __launch_bounds__(kCellBlock) k_residual(TopoView t, const R* __restrict__ fflux,
-                                                         double* __restrict__ Un, double* __restrict__ Unp1,
-                                                         R* __restrict__ W, double* __restrict__ res_out, double dt,
-                                                         int stage) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= t.C) return;
+__device__ __forceinline__ void residual_cell(const TopoView& t, const R* __restrict__ fflux, double* __restrict__ Un,
+                                              double* __restrict__ Unp1, R* __restrict__ W,
+                                              double* __restrict__ res_out, double dt, int stage, int c) {
   const int C = t.C;
   double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
 #pragma unroll 1
@@ -289,7 +332,8 @@ __global__ void __launch_bounds__(kCellBlock) k_residual(TopoView t, const R* __
     case 2: beta = 1.0 / 3.0; alpha_next = 1.0; break;
     default: beta = 1.0 / 6.0; alpha_next = 0.0; break;
   }
-  const double dtv = dt / t.vol[c];
+  // dt/V as the reference rounds it; the mixed form multiplies by 1/V.
+  const double dtv = std::is_same<R, double>::value ? dt / t.vol[c] : dt * t.vinv[c];
   double ut[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
@@ -309,10 +353,93 @@ __global__ void __launch_bounds__(kCellBlock) k_residual(TopoView t, const R* __
       ut[k] = u1 + alpha_next * r;
     }
   }
-  double v[5];
-  primitives(ut, v);
-#pragma unroll
-  for (int k = 0; k < 5; ++k) W[k * C + c] = static_cast<R>(v[k]);
+  store_primitives<R>(ut, W, C, c);
+}
+
+
+// ---- single-mesh kernels: one thread per cell / face ----
+template <class R, int MODE>
+__global__ void __launch_bounds__(kCellBlock) k_sweep1(TopoView t, GeomView<R> g, const R* __restrict__ W,
+                                                       R* __restrict__ grad, R* __restrict__ phi) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < t.C) sweep1_cell<R, MODE>(t, g, W, grad, phi, c);
+}
+
+template <class R, bool SECOND, bool VISC>
+__global__ void __launch_bounds__(kFaceBlock) k_internal_flux(TopoView t, GeomView<R> g, const R* __restrict__ W,
+                                                              const R* __restrict__ grad, const R* __restrict__ phi,
+                                                              Transport tr, R* __restrict__ fflux) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f < t.Fi) internal_flux_face<R, SECOND, VISC>(t, g, W, grad, phi, tr, fflux, f);
+}
+
+template <class R>
+__global__ void __launch_bounds__(kFaceBlock) k_bc_flux(TopoView t, GeomView<R> g, const R* __restrict__ W,
+                                                        Transport tr, InflowState inflow, R* __restrict__ fflux) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < t.Fb) bc_flux_face<R>(t, g, W, tr, inflow, fflux, i);
+}
+
+template <class R>
+__global__ void __launch_bounds__(kCellBlock) k_residual(TopoView t, const R* __restrict__ fflux,
+                                                         double* __restrict__ Un, double* __restrict__ Unp1,
+                                                         R* __restrict__ W, double* __restrict__ res_out, double dt,
+                                                         int stage) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < t.C) residual_cell<R>(t, fflux, Un, Unp1, W, res_out, dt, stage, c);
+}
+
+// ---- batched kernels: persistent grid over chunks of (segment, first item) ----
+// Each block takes whole chunks; a chunk holds blockDim.x consecutive items of
+// one segment. The chunk count is read from device memory so that a captured
+// graph stays valid when the batch membership changes.
+template <class R, int MODE>
+__global__ void __launch_bounds__(256) kb_sweep1(const Segment<R>* __restrict__ segs, const int2* __restrict__ chunks,
+                                                 const int* __restrict__ nchunks) {
+  const int n = *nchunks;
+  for (int ch = blockIdx.x; ch < n; ch += gridDim.x) {
+    const int2 cs = chunks[ch];
+    const Segment<R>& sg = segs[cs.x];
+    const int c = cs.y + threadIdx.x;
+    if (c < sg.t.C) sweep1_cell<R, MODE>(sg.t, sg.g, sg.b.W, sg.b.grad, sg.b.phi, c);
+  }
+}
+
+template <class R, bool SECOND, bool VISC>
+__global__ void __launch_bounds__(256) kb_internal_flux(const Segment<R>* __restrict__ segs,
+                                                        const int2* __restrict__ chunks,
+                                                        const int* __restrict__ nchunks, Transport tr) {
+  const int n = *nchunks;
+  for (int ch = blockIdx.x; ch < n; ch += gridDim.x) {
+    const int2 cs = chunks[ch];
+    const Segment<R>& sg = segs[cs.x];
+    const int f = cs.y + threadIdx.x;
+    if (f < sg.t.Fi) internal_flux_face<R, SECOND, VISC>(sg.t, sg.g, sg.b.W, sg.b.grad, sg.b.phi, tr, sg.b.fflux, f);
+  }
+}
+
+template <class R>
+__global__ void __launch_bounds__(256) kb_bc_flux(const Segment<R>* __restrict__ segs, const int2* __restrict__ chunks,
+                                                  const int* __restrict__ nchunks, Transport tr) {
+  const int n = *nchunks;
+  for (int ch = blockIdx.x; ch < n; ch += gridDim.x) {
+    const int2 cs = chunks[ch];
+    const Segment<R>& sg = segs[cs.x];
+    const int i = cs.y + threadIdx.x;
+    if (i < sg.t.Fb) bc_flux_face<R>(sg.t, sg.g, sg.b.W, tr, sg.inflow, sg.b.fflux, i);
+  }
+}
+
+template <class R>
+__global__ void __launch_bounds__(256) kb_residual(const Segment<R>* __restrict__ segs, const int2* __restrict__ chunks,
+                                                   const int* __restrict__ nchunks, int stage) {
+  const int n = *nchunks;
+  for (int ch = blockIdx.x; ch < n; ch += gridDim.x) {
+    const int2 cs = chunks[ch];
+    const Segment<R>& sg = segs[cs.x];
+    const int c = cs.y + threadIdx.x;
+    if (c < sg.t.C) residual_cell<R>(sg.t, sg.b.fflux, sg.s.Un, sg.s.Unp1, sg.b.W, sg.s.res, sg.dt, stage, c);
+  }
 }
 
 // Primitives of U_n + 0 * res with res = 0 (first stage after set_state).
@@ -323,9 +450,8 @@ __global__ void k_init_primitives(int C, const double* __restrict__ Un, R* __res
   double ut[5], v[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k) ut[k] = Un[k * C + c] + 0.0 * zero;
-  primitives(ut, v);
-#pragma unroll
-  for (int k = 0; k < 5; ++k) W[k * C + c] = static_cast<R>(v[k]);
+  (void)v;
+  store_primitives<R>(ut, W, C, c);
 }
 
 inline unsigned blocks_for(int n, int bs) { return static_cast<unsigned>((n + bs - 1) / bs); }

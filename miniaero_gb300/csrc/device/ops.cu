@@ -64,6 +64,54 @@ __global__ void k_op_primitives(int n, const double* U, double* V) {
   primitives(U + 5 * i, V + 5 * i);
 }
 
+__device__ __forceinline__ uint64_t splitmix64(uint64_t& s) {
+  uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// Double with random significand bits and a biased exponent in [e0, e0 + span).
+__device__ __forceinline__ double make_double(uint64_t r, int e0, int span, bool negative_ok) {
+  const uint64_t mant = r & 0x000FFFFFFFFFFFFFull;
+  const uint64_t e = static_cast<uint64_t>(e0 + static_cast<int>((r >> 52) % static_cast<uint64_t>(span)));
+  const uint64_t sign = (negative_ok && ((r >> 63) & 1)) ? (1ull << 63) : 0ull;
+  return __longlong_as_double(static_cast<long long>(sign | (e << 52) | mant));
+}
+
+// div_by_recip against the IEEE quotient on generated operand pairs.
+// mode 0: random a and b; 1: b with an all-ones significand (possibly a few
+// bits cleared); 2: quotients close to a rounding midpoint.
+__global__ void k_check_division(int mode, unsigned long long n, unsigned long long seed,
+                                 unsigned long long* mismatches, double* example) {
+  const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+  for (unsigned long long i = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; i < n;
+       i += stride) {
+    uint64_t st = seed ^ (i * 0xD1B54A32D192ED03ull);
+    const uint64_t r1 = splitmix64(st), r2 = splitmix64(st), r3 = splitmix64(st);
+    double a = make_double(r1, 1023 - 300, 600, true);
+    double b = make_double(r2, 1023 - 60, 120, false);
+    if (mode == 1) {
+      const uint64_t clear = (r3 & 7) ? (r3 >> 8) & ((1ull << (r3 & 7)) - 1) : 0ull;
+      b = __longlong_as_double(static_cast<long long>((__double_as_longlong(b) | 0x000FFFFFFFFFFFFFull) & ~clear));
+    } else if (mode == 2) {
+      const double m = make_double(r3, 1023 - 40, 80, true);
+      const double h = __longlong_as_double(static_cast<long long>(
+          (static_cast<uint64_t>(__double_as_longlong(m)) & 0x7FF0000000000000ull) - (53ull << 52)));
+      a = fma(b, m, b * h);  // a / b close to the midpoint between m and its successor
+    }
+    const double y = 1.0 / b;
+    const double q = div_by_recip(a, b, y);
+    const double ref = a / b;
+    if (__double_as_longlong(q) != __double_as_longlong(ref) && !(q == 0.0 && ref == 0.0)) {
+      if (atomicAdd(mismatches, 1ull) == 0ull) {
+        example[0] = a;
+        example[1] = b;
+      }
+    }
+  }
+}
+
 inline unsigned blocks_for(int n, int bs) { return static_cast<unsigned>((n + bs - 1) / bs); }
 
 }  // namespace
@@ -100,6 +148,12 @@ cudaError_t launch_op_limiter(int n, int kind, const double* dumax, const double
 cudaError_t launch_op_primitives(int n, const double* U, double* V, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
   k_op_primitives<<<blocks_for(n, 256), 256, 0, stream>>>(n, U, V);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_check_division(int mode, unsigned long long n, unsigned long long seed,
+                                  unsigned long long* mismatches, double* example, cudaStream_t stream) {
+  k_check_division<<<152 * 8, 256, 0, stream>>>(mode, n, seed, mismatches, example);
   return cudaGetLastError();
 }
 

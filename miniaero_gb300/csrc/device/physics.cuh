@@ -25,6 +25,23 @@ template <class R> __device__ __forceinline__ R dabs(R x);
 template <> __device__ __forceinline__ double dabs<double>(double x) { return fabs(x); }
 template <> __device__ __forceinline__ float dabs<float>(float x) { return fabsf(x); }
 
+// a / b rounded to nearest, given y = RN(1/b) computed once per divisor.
+// Method: q0 = RN(a*y) is within 1.5 ulp of a/b; one residual correction
+// q1 = RN(q0 + RN(a - b*q0)*y) is faithful (error <= 1/2 ulp + O(2^-104));
+// by Markstein's theorem (y correctly rounded, q1 faithful, binary64, no
+// underflow or overflow) RN(q1 + (a - b*q1)*y) is the correctly rounded
+// quotient. 1 multiply + 4 FMAs instead of a full division. A zero quotient
+// may carry the opposite sign to a/b; every use below adds the result to an
+// accumulator that starts at +0, where the sign of a zero term never shows.
+__device__ __forceinline__ double div_by_recip(double a, double b, double y) {
+  double q = a * y;
+  double r = fma(-q, b, a);
+  q = fma(r, y, q);
+  r = fma(-q, b, a);
+  return fma(r, y, q);
+}
+__device__ __forceinline__ float div_by_recip(float a, float /*b*/, float y) { return a * y; }
+
 // Conserved -> primitive (rho, u, v, w, T); always FP64 (the state is FP64).
 __device__ __forceinline__ void primitives(const double U[5], double V[5]) {
   const double gamma = 1.4;
@@ -155,13 +172,20 @@ struct Transport {
   int model;       // 0 Sutherland, 1 constant
   double mu;
   double prandtl;
+  double k;        // constant model: mu * 1006 / prandtl, rounded as on the device
 };
+
+inline Transport make_transport(int model, double mu, double prandtl) {
+  Transport t{model, mu, prandtl, 0.0};
+  if (model == 1) t.k = mu * 1006.0 / prandtl;
+  return t;
+}
 
 template <class R>
 __device__ __forceinline__ void transport(const Transport& tr, R T, R& mu, R& k) {
   if (tr.model == 1) {
     mu = R(tr.mu);
-    k = mu * R(1006.0) / R(tr.prandtl);
+    k = R(tr.k);
   } else {
     mu = R(1.458e-6) * T * dsqrt<R>(T) / (T + R(110.4));
     k = mu * R(1006.0) / R(0.71);
@@ -179,13 +203,16 @@ __device__ __forceinline__ void viscous_flux(const R g[5][3], const R prim[5], c
   for (int i = 0; i < 5; ++i) vflux[i] = R(0.0);
 #pragma unroll
   for (int i = 0; i < 3; ++i) div += g[i + 1][i];
+  // t_ij = S_ij - div*delta_ij/3. Off the diagonal the subtracted term is a
+  // signed zero, so t_ij = S_ij up to the sign of a zero, which cannot change
+  // the +0-started sums below; on the diagonal div/3 is rounded exactly.
+  const R div3 = div_by_recip(div * R(1), R(3.), R(1.0 / 3.0));
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-      const R delta = (i == j) ? R(1) : R(0);
       const R S = R(0.5) * (g[i + 1][j] + g[j + 1][i]);
-      const R tij = S - div * delta / R(3.);
+      const R tij = (i == j) ? S - div3 : S;
       vflux[1 + i] += (R(2) * mu * tij) * a[j];
       vflux[4] += (R(2) * mu * tij) * prim[i + 1] * a[j];
     }
@@ -209,6 +236,32 @@ __device__ __forceinline__ R venkat(R dumax, R dumin, R du, R deltax3) {
     phi = R(1);
   }
   return phi;
+}
+
+// Numerator and denominator of the Venkatakrishnan function, rounded exactly
+// as venkat() rounds them, normalised to n >= 0, d > 0 (both are negated
+// when du < 0, which is exact). Returns false where venkat() returns 1.
+__device__ __forceinline__ bool venkat_ratio(double dumax, double dumin, double du, double eps2, double& n,
+                                             double& d) {
+  if (du > 1e-40) {
+    n = (dumax * dumax + eps2) * du + 2 * du * du * dumax;
+    d = du * (dumax * dumax + 2 * du * du + dumax * du + eps2);
+    return true;
+  }
+  if (du < -1e-40) {
+    n = -((dumin * dumin + eps2) * du + 2 * du * du * dumin);
+    d = -(du * (dumin * dumin + 2 * du * du + dumin * du + eps2));
+    return true;
+  }
+  return false;
+}
+
+// Exact test n1/d1 < n2/d2 for d1, d2 > 0: compares n1*d2 with n2*d1 as
+// unevaluated sums p + e (p = RN(x*y), e = fma(x, y, -p) exact).
+__device__ __forceinline__ bool ratio_less(double n1, double d1, double n2, double d2) {
+  const double p1 = n1 * d2, p2 = n2 * d1;
+  if (p1 != p2) return p1 < p2;
+  return fma(n1, d2, -p1) < fma(n2, d1, -p2);
 }
 
 template <class R>

@@ -250,8 +250,11 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
       float* g32 = a.take<float>(19 * static_cast<size_t>(F));
       double* vol64 = const_cast<double*>(m.topo.vol);
       float* vol32 = a.take<float>(C);
-      auto assign = [&](auto& gv, auto* base, auto* vol) {
+      double* vinv64 = a.take<double>(C);
+      float* vinv32 = a.take<float>(C);
+      auto assign = [&](auto& gv, auto* base, auto* vol, auto* vinv) {
         gv.vol = vol;
+        gv.vinv = vinv;
         gv.fn = base;
         gv.fnu = base + 3 * static_cast<size_t>(F);
         gv.ftu = base + 6 * static_cast<size_t>(F);
@@ -260,8 +263,8 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
         gv.dL = base + 13 * static_cast<size_t>(F);
         gv.dR = base + 16 * static_cast<size_t>(F);
       };
-      assign(m.g64, g64, vol64);
-      assign(m.g32, g32, vol32);
+      assign(m.g64, g64, vol64, vinv64);
+      assign(m.g32, g32, vol32, vinv32);
     };
     ma_mesh probe;
     layout(probe);
@@ -273,6 +276,7 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
     m->dmem = a.base;
     m->bytes = bytes;
     cudaGetDevice(&m->device);
+    m->topo.vinv = m->g64.vinv;
     m->topo.C = C;
     m->topo.Fi = Fi;
     m->topo.Fb = Fb;
@@ -281,8 +285,13 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
 
     std::vector<float> geo32(geo.size());
     for (size_t i = 0; i < geo.size(); ++i) geo32[i] = static_cast<float>(geo[i]);
-    std::vector<float> vol32(C);
-    for (int32_t c = 0; c < C; ++c) vol32[c] = static_cast<float>(v->cell_volumes[c]);
+    std::vector<float> vol32(C), vinv32(C);
+    std::vector<double> vinv64(C);
+    for (int32_t c = 0; c < C; ++c) {
+      vol32[c] = static_cast<float>(v->cell_volumes[c]);
+      vinv64[c] = 1.0 / v->cell_volumes[c];
+      vinv32[c] = static_cast<float>(vinv64[c]);
+    }
     auto copy = [&](const void* dst, const void* src, size_t n) {
       return cudaMemcpy(const_cast<void*>(dst), src, n, cudaMemcpyHostToDevice);
     };
@@ -295,6 +304,8 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
     if (e == cudaSuccess) e = copy(m->g64.fn, geo.data(), sizeof(double) * geo.size());
     if (e == cudaSuccess) e = copy(m->g32.fn, geo32.data(), sizeof(float) * geo32.size());
     if (e == cudaSuccess) e = copy(m->g32.vol, vol32.data(), sizeof(float) * vol32.size());
+    if (e == cudaSuccess) e = copy(m->g64.vinv, vinv64.data(), sizeof(double) * vinv64.size());
+    if (e == cudaSuccess) e = copy(m->g32.vinv, vinv32.data(), sizeof(float) * vinv32.size());
     if (e != cudaSuccess) {
       cudaFree(m->dmem);
       delete m;
@@ -385,7 +396,7 @@ extern "C" ma_status ma_solver_create(ma_mesh* mesh, const ma_options* o, ma_sol
   s->cfg.second_order = o->second_order_space != 0;
   s->cfg.viscous = o->viscous != 0;
   s->cfg.limiter = o->limiter;
-  s->cfg.transport = dev::Transport{o->viscosity_model, o->mu, o->prandtl};
+  s->cfg.transport = dev::make_transport(o->viscosity_model, o->mu, o->prandtl);
   for (int k = 0; k < 5; ++k) s->cfg.inflow[k] = o->inflow_state[k];
   s->cfg.dt = o->dt;
   const size_t C = mesh->topo.C, F = mesh->topo.F;
@@ -689,7 +700,7 @@ extern "C" ma_status ma_op_viscous_flux(int32_t n, const double* grad, const dou
   MA_CUDA_TRY(b.in(prim, 5 * (size_t)n, &dp));
   MA_CUDA_TRY(b.in(area, 3 * (size_t)n, &da));
   MA_CUDA_TRY(b.in(nullptr, 5 * (size_t)n, &dv));
-  MA_CUDA_TRY(dev::launch_op_viscous(n, dg, dp, da, dev::Transport{viscosity_model, mu, prandtl}, dv, 0));
+  MA_CUDA_TRY(dev::launch_op_viscous(n, dg, dp, da, dev::make_transport(viscosity_model, mu, prandtl), dv, 0));
   MA_CUDA_TRY(cudaMemcpy(vflux, dv, sizeof(double) * 5 * n, cudaMemcpyDeviceToHost));
   return MA_OK;
 }
@@ -708,6 +719,23 @@ extern "C" ma_status ma_op_limiter(int32_t n, int32_t kind, const double* dumax,
   MA_CUDA_TRY(b.in(nullptr, n, &p));
   MA_CUDA_TRY(dev::launch_op_limiter(n, kind, a, bb, c, d, p, 0));
   MA_CUDA_TRY(cudaMemcpy(phi, p, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  return MA_OK;
+}
+
+extern "C" ma_status ma_debug_check_division(int32_t mode, uint64_t n, uint64_t seed, uint64_t* mismatches,
+                                             double* example) {
+  if (!mismatches || !example || mode < 0 || mode > 2) return set_error(MA_EINVAL, "ma_debug_check_division: bad arguments");
+  DevBufs b;
+  double* dex;
+  MA_CUDA_TRY(b.in(nullptr, 3, &dex));
+  unsigned long long* dm = reinterpret_cast<unsigned long long*>(dex + 2);
+  MA_CUDA_TRY(cudaMemset(dex, 0, 3 * sizeof(double)));
+  MA_CUDA_TRY(dev::launch_check_division(mode, n, seed, dm, dex, 0));
+  double host[3];
+  MA_CUDA_TRY(cudaMemcpy(host, dex, sizeof(host), cudaMemcpyDeviceToHost));
+  std::memcpy(mismatches, &host[2], sizeof(uint64_t));
+  example[0] = host[0];
+  example[1] = host[1];
   return MA_OK;
 }
 

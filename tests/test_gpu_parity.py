@@ -215,3 +215,15 @@ def test_mixed_flat_plate_density_error(has_gpu):
     om.precision = ma.MA_PREC_MIXED
     Um = run_gpu(md, om, U0)
     assert rel_l2(Um[:, 0], ref[:, 0]) < 1e-5
+
+
+# ---- exact division used by the gradient ------------------------------------------------
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_reciprocal_division_is_correctly_rounded(has_gpu, mode):
+    """div_by_recip(a, b, RN(1/b)) equals the IEEE quotient a/b (2^28 pairs per mode)."""
+    import ctypes
+    from miniaero_gb300 import _lib
+    mism = ctypes.c_uint64(0)
+    ex = np.zeros(2)
+    _lib.check(_lib.lib().ma_debug_check_division(mode, 1 << 28, 12345 + mode, ctypes.byref(mism), _lib.f64p(ex)))
+    assert mism.value == 0, "first mismatch a=%r b=%r" % (ex[0], ex[1])

@@ -180,6 +180,105 @@ ma_status ma_solver_check_state(ma_solver* s, int64_t* bad_cell);
 /* One full solve as the reference's Solve(): init + ntimesteps steps. */
 ma_status ma_solver_solve(ma_solver* s, const ma_host_mesh* host_mesh);
 
+/* ---- batched multi-mesh solver ------------------------------------------
+ * No reference counterpart as an API: the reference advances one mesh per
+ * process (Solve(), TimeSolverExplicitRK4.h:206) and scales out with MPI
+ * ranks; here independent meshes of uneven size share one device and advance
+ * together, one persistent launch per kernel kind and stage for the whole
+ * batch, captured in a CUDA graph. Physics options (order, viscosity,
+ * limiter, precision) are per batch; time step and inflow state per member.
+ * A member's result is bit-identical to the same solve run alone. */
+typedef struct ma_batch ma_batch;
+/* capacity: maximum members; budget_bytes: device bytes members may hold. */
+ma_status ma_batch_create(const ma_options* physics, int32_t capacity, size_t budget_bytes, ma_batch** out);
+void ma_batch_free(ma_batch* b);
+/* Device bytes a member on this mesh would hold (budget accounting). */
+size_t ma_batch_member_bytes(const ma_batch* b, const ma_mesh* mesh);
+/* Adds a member with initial state U0. dt > 0 fixes the time step; dt <= 0
+ * takes it from physics->cfl on U0. inflow_state (5 conserved values) may be
+ * NULL for physics->inflow_state. MA_EBUDGET when it does not fit. The mesh
+ * must outlive the member. */
+ma_status ma_batch_add(ma_batch* b, ma_mesh* mesh, const double* U0, int32_t layout, double dt,
+                       const double* inflow_state, int32_t* member_id);
+ma_status ma_batch_remove(ma_batch* b, int32_t member_id);
+ma_status ma_batch_get_state(ma_batch* b, int32_t member_id, double* U, int32_t layout);
+/* Advances every member nsteps RK4 steps (asynchronous). */
+ma_status ma_batch_step(ma_batch* b, int32_t nsteps);
+ma_status ma_batch_synchronize(ma_batch* b);
+void* ma_batch_stream(ma_batch* b);
+int64_t ma_batch_cells(ma_batch* b);
+int32_t ma_batch_size(const ma_batch* b);
+size_t ma_batch_device_bytes(const ma_batch* b);
+int64_t ma_batch_member_steps(const ma_batch* b, int32_t member_id);
+double ma_batch_member_dt(const ma_batch* b, int32_t member_id);
+/* Launch shapes per kernel kind (MA_KERNEL_*): threads per block (= items per
+ * chunk) and persistent grid size. */
+ma_status ma_batch_get_launch(const ma_batch* b, int32_t* block, int32_t* grid);
+ma_status ma_batch_set_launch(ma_batch* b, const int32_t* block, const int32_t* grid);
+/* Autotuner: times each kernel kind over the current members for block sizes
+ * 64/128/256 x 1..16 CTAs per SM and keeps the fastest; member states are
+ * restored afterwards. best_ms (4 values, may be NULL) receives the chosen
+ * per-launch times. */
+ma_status ma_batch_autotune(ma_batch* b, int32_t reps, double* best_ms);
+
+/* ---- serving loop -------------------------------------------------------
+ * No reference counterpart: the reference runs one solve per invocation
+ * (Main.C:96-151). The server admits solve requests first-in first-out while
+ * their device memory (member state + cached device mesh) fits the budget,
+ * keeps their state resident, and advances all running requests together in
+ * ticks of the batch solver (continuous batching: arrivals join at the next
+ * tick, finished requests leave). Every request's result equals the same
+ * solve run alone. */
+typedef struct ma_server ma_server;
+enum { MA_SERVER_THREAD = 1,   /* run the scheduling loop on a server thread */
+       MA_SERVER_DRYRUN = 2 }; /* no device work: sizes and ticks only (host tests) */
+enum { MA_REQ_QUEUED = 0, MA_REQ_RUNNING = 1, MA_REQ_DONE = 2, MA_REQ_CANCELLED = 3, MA_REQ_FAILED = 4 };
+typedef struct {
+  int32_t nx, ny, nz;          /* box mesh cells per axis */
+  int32_t problem_type;        /* selects the BC map (Parallel3DMesh.h:382-396) */
+  double lx, ly, lz, angle;
+  double inflow_state[5];      /* conserved inflow state, also the initial state */
+  int32_t nsteps;              /* RK4 steps to run */
+  double dt;                   /* > 0: fixed; <= 0: from the server's physics.cfl */
+  int32_t keep_result;         /* 1: keep the final state for ma_server_result */
+} ma_request;
+typedef struct {
+  int32_t state;               /* MA_REQ_* */
+  int32_t error;               /* ma_status of a failed request */
+  int64_t steps_done;
+  int64_t cells;
+  int64_t t_submit_ns, t_admit_ns, t_finish_ns;  /* since server creation */
+  double state_sq_norm[5];     /* sum over cells of U_k^2 of the final state */
+} ma_request_info;
+typedef struct {
+  int64_t submitted, admitted, completed, failed, cancelled;
+  int64_t ticks, cell_stages;
+  int64_t bytes_in_use, peak_bytes;
+  int32_t running, queued, peak_running, capacity, cached_meshes;
+  double busy_seconds;         /* time with at least one request running */
+} ma_server_stats;
+/* physics: options shared by all requests (order, viscosity, limiter,
+ * precision, cfl); budget_bytes: device bytes for states and meshes;
+ * tick_steps: RK4 steps per scheduling tick; capacity: max running requests. */
+ma_status ma_server_create(const ma_options* physics, size_t budget_bytes, int32_t tick_steps, int32_t capacity,
+                           int32_t flags, ma_server** out);
+void ma_server_free(ma_server* s);
+/* Thread-safe; returns at once with the request id. */
+ma_status ma_server_submit(ma_server* s, const ma_request* r, int64_t* id);
+/* Builds and caches the device mesh a request of this shape would use. */
+ma_status ma_server_preload_mesh(ma_server* s, const ma_request* r);
+/* One scheduling iteration (admit, tick, retire) when the server has no
+ * thread of its own; *progressed = 0 when nothing ran. */
+ma_status ma_server_poll(ma_server* s, int32_t* progressed);
+ma_status ma_server_cancel(ma_server* s, int64_t id);
+ma_status ma_server_query(ma_server* s, int64_t id, ma_request_info* info);
+/* Final state (AOS) of a finished request that set keep_result. */
+ma_status ma_server_result(ma_server* s, int64_t id, double* U);
+/* Waits until the request leaves the queue/running states or timeout_s
+ * passes (MA_ETIMEDOUT). Without a server thread it drives the loop itself. */
+ma_status ma_server_wait(ma_server* s, int64_t id, double timeout_s);
+ma_status ma_server_get_stats(ma_server* s, ma_server_stats* out);
+
 /* ---- diagnostics (host only) -------------------------------------------- */
 /* First n outputs of the glibc rand() sequence for seed (the generator behind
  * std::random_shuffle in Parallel3DMesh.h:362). */

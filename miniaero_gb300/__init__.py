@@ -315,6 +315,171 @@ class TimeSolverExplicitRK4:
         self.close()
 
 
+class Batch:
+    """Many independent meshes advanced together (ma_batch_*)."""
+
+    def __init__(self, physics, capacity=256, budget_bytes=150 << 30):
+        self.physics = physics.copy()
+        self._h = ctypes.c_void_p()
+        check(lib().ma_batch_create(ctypes.byref(self.physics.c), int(capacity), int(budget_bytes),
+                                    ctypes.byref(self._h)))
+        self._meshes = {}
+
+    def member_bytes(self, device_mesh):
+        return int(lib().ma_batch_member_bytes(self._h, device_mesh._h))
+
+    def add(self, device_mesh, U0, dt=0.0, inflow_state=None):
+        U0 = np.ascontiguousarray(U0, dtype=np.float64).reshape(device_mesh.ncells, 5)
+        mid = ctypes.c_int32(-1)
+        inflow = None
+        if inflow_state is not None:
+            inflow = np.ascontiguousarray(inflow_state, dtype=np.float64).reshape(5)
+        check(lib().ma_batch_add(self._h, device_mesh._h, f64p(U0), MA_LAYOUT_AOS, float(dt),
+                                 f64p(inflow) if inflow is not None else ctypes.cast(None, _lib.P_f64),
+                                 ctypes.byref(mid)))
+        self._meshes[mid.value] = device_mesh  # keep the mesh alive
+        return mid.value
+
+    def remove(self, member_id):
+        check(lib().ma_batch_remove(self._h, int(member_id)))
+        self._meshes.pop(member_id, None)
+
+    def get_state(self, member_id):
+        dm = self._meshes[member_id]
+        U = np.empty((dm.ncells, 5), np.float64)
+        check(lib().ma_batch_get_state(self._h, int(member_id), f64p(U), MA_LAYOUT_AOS))
+        return U
+
+    def step(self, nsteps=1):
+        check(lib().ma_batch_step(self._h, int(nsteps)))
+
+    def synchronize(self):
+        check(lib().ma_batch_synchronize(self._h))
+
+    def autotune(self, reps=3):
+        best = np.zeros(4)
+        check(lib().ma_batch_autotune(self._h, int(reps), f64p(best)))
+        return best
+
+    @property
+    def launch(self):
+        b = np.zeros(4, np.int32)
+        g = np.zeros(4, np.int32)
+        check(lib().ma_batch_get_launch(self._h, i32p(b), i32p(g)))
+        return b.tolist(), g.tolist()
+
+    def set_launch(self, block, grid):
+        b = np.ascontiguousarray(block, np.int32)
+        g = np.ascontiguousarray(grid, np.int32)
+        check(lib().ma_batch_set_launch(self._h, i32p(b), i32p(g)))
+
+    def member_dt(self, member_id):
+        return float(lib().ma_batch_member_dt(self._h, int(member_id)))
+
+    def member_steps(self, member_id):
+        return int(lib().ma_batch_member_steps(self._h, int(member_id)))
+
+    @property
+    def stream(self):
+        return lib().ma_batch_stream(self._h)
+
+    @property
+    def cells(self):
+        return int(lib().ma_batch_cells(self._h))
+
+    @property
+    def size(self):
+        return int(lib().ma_batch_size(self._h))
+
+    @property
+    def device_bytes(self):
+        return int(lib().ma_batch_device_bytes(self._h))
+
+    def close(self):
+        if self._h:
+            lib().ma_batch_free(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Serving loop with continuous batching (ma_server_*)."""
+
+    QUEUED, RUNNING, DONE, CANCELLED, FAILED = range(5)
+
+    def __init__(self, physics, budget_bytes=150 << 30, tick_steps=10, capacity=512, thread=True, dry_run=False):
+        self.physics = physics.copy()
+        flags = (_lib.MA_SERVER_THREAD if thread else 0) | (_lib.MA_SERVER_DRYRUN if dry_run else 0)
+        self._h = ctypes.c_void_p()
+        check(lib().ma_server_create(ctypes.byref(self.physics.c), int(budget_bytes), int(tick_steps), int(capacity),
+                                     flags, ctypes.byref(self._h)))
+        self._cells = {}
+
+    @staticmethod
+    def request(nx, ny, nz, lx, ly, lz, inflow_state, nsteps, problem_type=1, dt=0.0, keep_result=False, angle=0.0):
+        r = _lib.ma_request()
+        r.nx, r.ny, r.nz, r.problem_type = int(nx), int(ny), int(nz), int(problem_type)
+        r.lx, r.ly, r.lz, r.angle = float(lx), float(ly), float(lz), float(angle)
+        for k in range(5):
+            r.inflow_state[k] = float(inflow_state[k])
+        r.nsteps = int(nsteps)
+        r.dt = float(dt)
+        r.keep_result = 1 if keep_result else 0
+        return r
+
+    def submit(self, req):
+        rid = ctypes.c_int64(-1)
+        check(lib().ma_server_submit(self._h, ctypes.byref(req), ctypes.byref(rid)))
+        self._cells[rid.value] = req.nx * req.ny * req.nz
+        return rid.value
+
+    def preload(self, req):
+        check(lib().ma_server_preload_mesh(self._h, ctypes.byref(req)))
+
+    def poll(self):
+        p = ctypes.c_int32(0)
+        check(lib().ma_server_poll(self._h, ctypes.byref(p)))
+        return bool(p.value)
+
+    def cancel(self, rid):
+        check(lib().ma_server_cancel(self._h, int(rid)))
+
+    def query(self, rid):
+        info = _lib.ma_request_info()
+        check(lib().ma_server_query(self._h, int(rid), ctypes.byref(info)))
+        return info
+
+    def wait(self, rid, timeout=60.0):
+        check(lib().ma_server_wait(self._h, int(rid), float(timeout)))
+        return self.query(rid)
+
+    def result(self, rid):
+        U = np.empty((self._cells[rid], 5), np.float64)
+        check(lib().ma_server_result(self._h, int(rid), f64p(U)))
+        return U
+
+    def stats(self):
+        st = _lib.ma_server_stats()
+        check(lib().ma_server_get_stats(self._h, ctypes.byref(st)))
+        return {n: getattr(st, n) for n, _ in st._fields_}
+
+    def close(self):
+        if self._h:
+            lib().ma_server_free(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 # ---- operator-level entry points -------------------------------------------------
 def _a(x, shape):
     return np.ascontiguousarray(x, dtype=np.float64).reshape(shape)

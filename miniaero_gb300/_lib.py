@@ -80,6 +80,42 @@ class ma_mesh_view(ctypes.Structure):
     ]
 
 
+class ma_request(ctypes.Structure):
+    _fields_ = [
+        ("nx", c_int32), ("ny", c_int32), ("nz", c_int32), ("problem_type", c_int32),
+        ("lx", c_double), ("ly", c_double), ("lz", c_double), ("angle", c_double),
+        ("inflow_state", c_double * 5),
+        ("nsteps", c_int32),
+        ("dt", c_double),
+        ("keep_result", c_int32),
+    ]
+
+
+class ma_request_info(ctypes.Structure):
+    _fields_ = [
+        ("state", c_int32), ("error", c_int32),
+        ("steps_done", ctypes.c_int64), ("cells", ctypes.c_int64),
+        ("t_submit_ns", ctypes.c_int64), ("t_admit_ns", ctypes.c_int64), ("t_finish_ns", ctypes.c_int64),
+        ("state_sq_norm", c_double * 5),
+    ]
+
+
+class ma_server_stats(ctypes.Structure):
+    _fields_ = [
+        ("submitted", ctypes.c_int64), ("admitted", ctypes.c_int64), ("completed", ctypes.c_int64),
+        ("failed", ctypes.c_int64), ("cancelled", ctypes.c_int64),
+        ("ticks", ctypes.c_int64), ("cell_stages", ctypes.c_int64),
+        ("bytes_in_use", ctypes.c_int64), ("peak_bytes", ctypes.c_int64),
+        ("running", c_int32), ("queued", c_int32), ("peak_running", c_int32), ("capacity", c_int32),
+        ("cached_meshes", c_int32),
+        ("busy_seconds", c_double),
+    ]
+
+
+MA_SERVER_THREAD, MA_SERVER_DRYRUN = 1, 2
+MA_REQ_QUEUED, MA_REQ_RUNNING, MA_REQ_DONE, MA_REQ_CANCELLED, MA_REQ_FAILED = range(5)
+
+
 class MiniaeroError(RuntimeError):
     """A C-ABI call returned a non-zero ma_status."""
 
@@ -121,6 +157,34 @@ _SIGNATURES = {
     "ma_solver_set_dt": (c_int32, [c_void_p, c_double]),
     "ma_solver_check_state": (c_int32, [c_void_p, ctypes.POINTER(ctypes.c_int64)]),
     "ma_solver_solve": (c_int32, [c_void_p, c_void_p]),
+    "ma_batch_create": (c_int32, [ctypes.POINTER(ma_options), c_int32, ctypes.c_size_t, ctypes.POINTER(c_void_p)]),
+    "ma_batch_free": (None, [c_void_p]),
+    "ma_batch_member_bytes": (ctypes.c_size_t, [c_void_p, c_void_p]),
+    "ma_batch_add": (c_int32, [c_void_p, c_void_p, P_f64, c_int32, c_double, P_f64, P_i32]),
+    "ma_batch_remove": (c_int32, [c_void_p, c_int32]),
+    "ma_batch_get_state": (c_int32, [c_void_p, c_int32, P_f64, c_int32]),
+    "ma_batch_step": (c_int32, [c_void_p, c_int32]),
+    "ma_batch_synchronize": (c_int32, [c_void_p]),
+    "ma_batch_stream": (c_void_p, [c_void_p]),
+    "ma_batch_cells": (ctypes.c_int64, [c_void_p]),
+    "ma_batch_size": (c_int32, [c_void_p]),
+    "ma_batch_device_bytes": (ctypes.c_size_t, [c_void_p]),
+    "ma_batch_member_steps": (ctypes.c_int64, [c_void_p, c_int32]),
+    "ma_batch_member_dt": (c_double, [c_void_p, c_int32]),
+    "ma_batch_get_launch": (c_int32, [c_void_p, P_i32, P_i32]),
+    "ma_batch_set_launch": (c_int32, [c_void_p, P_i32, P_i32]),
+    "ma_batch_autotune": (c_int32, [c_void_p, c_int32, P_f64]),
+    "ma_server_create": (c_int32, [ctypes.POINTER(ma_options), ctypes.c_size_t, c_int32, c_int32, c_int32,
+                                   ctypes.POINTER(c_void_p)]),
+    "ma_server_free": (None, [c_void_p]),
+    "ma_server_submit": (c_int32, [c_void_p, ctypes.POINTER(ma_request), ctypes.POINTER(ctypes.c_int64)]),
+    "ma_server_preload_mesh": (c_int32, [c_void_p, ctypes.POINTER(ma_request)]),
+    "ma_server_poll": (c_int32, [c_void_p, P_i32]),
+    "ma_server_cancel": (c_int32, [c_void_p, ctypes.c_int64]),
+    "ma_server_query": (c_int32, [c_void_p, ctypes.c_int64, ctypes.POINTER(ma_request_info)]),
+    "ma_server_result": (c_int32, [c_void_p, ctypes.c_int64, P_f64]),
+    "ma_server_wait": (c_int32, [c_void_p, ctypes.c_int64, c_double]),
+    "ma_server_get_stats": (c_int32, [c_void_p, ctypes.POINTER(ma_server_stats)]),
     "ma_debug_glibc_rand": (c_int32, [ctypes.c_uint32, c_int32, P_i32]),
     "ma_debug_binsort": (c_int32, [P_i32, c_int32, P_i32]),
     "ma_debug_check_division": (c_int32, [c_int32, ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64),

@@ -33,8 +33,9 @@ DEVICE_SOURCES = [
     ("device/kernels_mixed.cu", ["--fmad=true"]),
     ("device/ops.cu", ["--fmad=false"]),
     ("device/solver.cu", ["--fmad=false"]),
+    ("device/batch.cu", ["--fmad=false"]),
 ]
-HOST_SOURCES = ["host/mesh.cpp", "host/options.cpp", "host/host_api.cpp"]
+HOST_SOURCES = ["host/mesh.cpp", "host/options.cpp", "host/host_api.cpp", "host/server.cpp"]
 
 
 def _nvcc():
@@ -77,7 +78,7 @@ def build(verbose=False, ptxas_info=False):
         for out in ex.map(lambda c: _run(c, verbose), jobs):
             outputs.append(out)
     objs = [_obj(s) for s, _ in DEVICE_SOURCES] + [_obj(s) for s in HOST_SOURCES]
-    _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-cudart", "static"], verbose)
+    _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-cudart", "static", "-lpthread"], verbose)
     _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", os.path.join(CSRC, "cli", "main.cpp"),
           "-o", CLI, "-L" + BUILD, "-lminiaero_gpu", "-Wl,-rpath,$ORIGIN"], verbose)
     if ptxas_info:

@@ -1,0 +1,18 @@
+// Accessors of ma_mesh (defined in solver.cu) for the batch and server code.
+#pragma once
+#include <cstddef>
+
+#include "../../../include/miniaero_gpu.h"
+#include "kernels.cuh"
+
+namespace miniaero {
+size_t mesh_cells(const ma_mesh* m);
+size_t mesh_faces(const ma_mesh* m);
+dev::TopoView mesh_topo(const ma_mesh* m);
+template <class R>
+dev::GeomView<R> mesh_geom(const ma_mesh* m);
+template <>
+dev::GeomView<double> mesh_geom<double>(const ma_mesh* m);
+template <>
+dev::GeomView<float> mesh_geom<float>(const ma_mesh* m);
+}  // namespace miniaero

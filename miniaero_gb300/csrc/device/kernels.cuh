@@ -111,6 +111,31 @@ template <>
 cudaError_t launch_stage<float>(const TopoView&, const GeomView<float>&, const PathConfig&, const StateBuffers&,
                                 const StageBuffers<float>&, int, cudaStream_t, unsigned);
 
+// Batched stage over segments: chunks[k] lists (segment, first item) pairs of
+// kernel kind k (sweep, internal flux, boundary flux, residual), each chunk
+// covering block[k] items; nchunks is a device array of 4 counts.
+struct BatchLaunch {
+  const int2* chunks[4] = {nullptr, nullptr, nullptr, nullptr};
+  const int* nchunks = nullptr;  // device [4]
+  int block[4] = {128, 128, 128, 128};
+  int grid[4] = {1, 1, 1, 1};
+};
+
+template <class R>
+cudaError_t launch_batch_stage(const PathConfig& cfg, const Segment<R>* segs, const BatchLaunch& bl, int stage,
+                               cudaStream_t stream, unsigned kernels = kAllKernels);
+template <>
+cudaError_t launch_batch_stage<double>(const PathConfig&, const Segment<double>*, const BatchLaunch&, int,
+                                       cudaStream_t, unsigned);
+template <>
+cudaError_t launch_batch_stage<float>(const PathConfig&, const Segment<float>*, const BatchLaunch&, int,
+                                      cudaStream_t, unsigned);
+
+// dt bound of the CFL rule: writes min_c V_c / sum_f(|u.n| + c|n|) (as the
+// bits of a positive double) into *out via atomicMin; *out must start at ~0.
+cudaError_t launch_cfl(const TopoView& t, const GeomView<double>& g, const double* Un, unsigned long long* out,
+                       cudaStream_t stream);
+
 // Operator-level kernels (unit parity, FP64).
 cudaError_t launch_op_roe(int n, const double* pl, const double* pr, const double* normal, const double* tangent,
                           const double* binormal, double* flux, cudaStream_t stream);

@@ -18,5 +18,11 @@ cudaError_t launch_stage<double>(const TopoView& t, const GeomView<double>& g, c
   return launch_stage_impl<double>(t, g, cfg, s, b, stage, stream, kernels);
 }
 
+template <>
+cudaError_t launch_batch_stage<double>(const PathConfig& cfg, const Segment<double>* segs, const BatchLaunch& bl,
+                                   int stage, cudaStream_t stream, unsigned kernels) {
+  return launch_batch_stage_impl<double>(cfg, segs, bl, stage, stream, kernels);
+}
+
 }  // namespace dev
 }  // namespace miniaero

@@ -502,6 +502,39 @@ cudaError_t launch_stage_impl(const TopoView& t, const GeomView<R>& g, const Pat
   return cudaGetLastError();
 }
 
+template <class R>
+cudaError_t launch_batch_stage_impl(const PathConfig& cfg, const Segment<R>* segs, const BatchLaunch& bl, int stage,
+                                    cudaStream_t stream, unsigned kernels) {
+  const Transport tr = cfg.transport;
+  if ((kernels & kSweep1) && (cfg.second_order || cfg.viscous)) {
+    const dim3 g(bl.grid[0]), b(bl.block[0]);
+    if (!cfg.second_order)
+      kb_sweep1<R, 0><<<g, b, 0, stream>>>(segs, bl.chunks[0], bl.nchunks + 0);
+    else if (cfg.limiter == 1)
+      kb_sweep1<R, 2><<<g, b, 0, stream>>>(segs, bl.chunks[0], bl.nchunks + 0);
+    else
+      kb_sweep1<R, 1><<<g, b, 0, stream>>>(segs, bl.chunks[0], bl.nchunks + 0);
+  }
+  if (kernels & kInternalFlux) {
+    const dim3 g(bl.grid[1]), b(bl.block[1]);
+    if (cfg.second_order) {
+      if (cfg.viscous)
+        kb_internal_flux<R, true, true><<<g, b, 0, stream>>>(segs, bl.chunks[1], bl.nchunks + 1, tr);
+      else
+        kb_internal_flux<R, true, false><<<g, b, 0, stream>>>(segs, bl.chunks[1], bl.nchunks + 1, tr);
+    } else {
+      if (cfg.viscous)
+        kb_internal_flux<R, false, true><<<g, b, 0, stream>>>(segs, bl.chunks[1], bl.nchunks + 1, tr);
+      else
+        kb_internal_flux<R, false, false><<<g, b, 0, stream>>>(segs, bl.chunks[1], bl.nchunks + 1, tr);
+    }
+  }
+  if (kernels & kBcFlux) kb_bc_flux<R><<<bl.grid[2], bl.block[2], 0, stream>>>(segs, bl.chunks[2], bl.nchunks + 2, tr);
+  if (kernels & kResidual)
+    kb_residual<R><<<bl.grid[3], bl.block[3], 0, stream>>>(segs, bl.chunks[3], bl.nchunks + 3, stage);
+  return cudaGetLastError();
+}
+
 }  // namespace
 }  // namespace dev
 }  // namespace miniaero

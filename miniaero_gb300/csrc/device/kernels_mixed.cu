@@ -18,5 +18,11 @@ cudaError_t launch_stage<float>(const TopoView& t, const GeomView<float>& g, con
   return launch_stage_impl<float>(t, g, cfg, s, b, stage, stream, kernels);
 }
 
+template <>
+cudaError_t launch_batch_stage<float>(const PathConfig& cfg, const Segment<float>* segs, const BatchLaunch& bl,
+                                   int stage, cudaStream_t stream, unsigned kernels) {
+  return launch_batch_stage_impl<float>(cfg, segs, bl, stage, stream, kernels);
+}
+
 }  // namespace dev
 }  // namespace miniaero

@@ -112,6 +112,28 @@ __global__ void k_check_division(int mode, unsigned long long n, unsigned long l
   }
 }
 
+// dt = cfl * min_c V_c / sum_f (|u.n| + c |n|) on the current U_n.
+__global__ void k_cfl(TopoView t, GeomView<double> g, const double* __restrict__ Un,
+                      unsigned long long* out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= t.C) return;
+  const int C = t.C, F = t.F;
+  double U[5], V[5];
+  for (int k = 0; k < 5; ++k) U[k] = Un[k * C + c];
+  primitives(U, V);
+  const double a = sqrt(1.4 * 287.05 * V[4]);
+  double sum = 0.0;
+  for (int s = 0; s < kMaxCellFaces; ++s) {
+    const int code = t.csr_grad[s * C + c];
+    if (code < 0) continue;
+    const int f = code >> 1;
+    const double un = V[1] * g.fn[f] + V[2] * g.fn[F + f] + V[3] * g.fn[2 * F + f];
+    sum += fabs(un) + a * g.fnn[f];
+  }
+  const double r = t.vol[c] / sum;
+  if (r > 0.0) atomicMin(out, static_cast<unsigned long long>(__double_as_longlong(r)));
+}
+
 inline unsigned blocks_for(int n, int bs) { return static_cast<unsigned>((n + bs - 1) / bs); }
 
 }  // namespace
@@ -154,6 +176,13 @@ cudaError_t launch_op_primitives(int n, const double* U, double* V, cudaStream_t
 cudaError_t launch_check_division(int mode, unsigned long long n, unsigned long long seed,
                                   unsigned long long* mismatches, double* example, cudaStream_t stream) {
   k_check_division<<<152 * 8, 256, 0, stream>>>(mode, n, seed, mismatches, example);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cfl(const TopoView& t, const GeomView<double>& g, const double* Un, unsigned long long* out,
+                       cudaStream_t stream) {
+  if (t.C <= 0) return cudaSuccess;
+  k_cfl<<<blocks_for(t.C, 256), 256, 0, stream>>>(t, g, Un, out);
   return cudaGetLastError();
 }
 

@@ -20,6 +20,7 @@
 
 #include "../../../include/miniaero_gpu.h"
 #include "../host/errors.hpp"
+#include "batch_internal.hpp"
 #include "kernels.cuh"
 
 using miniaero::set_error;
@@ -318,6 +319,16 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
   }
 }
 
+namespace miniaero {
+size_t mesh_cells(const ma_mesh* m) { return static_cast<size_t>(m->topo.C); }
+size_t mesh_faces(const ma_mesh* m) { return static_cast<size_t>(m->topo.F); }
+dev::TopoView mesh_topo(const ma_mesh* m) { return m->topo; }
+template <>
+dev::GeomView<double> mesh_geom<double>(const ma_mesh* m) { return m->g64; }
+template <>
+dev::GeomView<float> mesh_geom<float>(const ma_mesh* m) { return m->g32; }
+}  // namespace miniaero
+
 extern "C" void ma_mesh_free(ma_mesh* m) {
   if (!m) return;
   cudaFree(m->dmem);
@@ -352,28 +363,6 @@ ma_status capture_step_graph(ma_solver* s) {
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return set_error(MA_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
   return MA_OK;
-}
-
-// dt = cfl * min_c V_c / sum_f (|u.n| + c |n|) on the current U_n.
-__global__ void k_cfl(dev::TopoView t, dev::GeomView<double> g, const double* __restrict__ Un,
-                      unsigned long long* out) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= t.C) return;
-  const int C = t.C, F = t.F;
-  double U[5], V[5];
-  for (int k = 0; k < 5; ++k) U[k] = Un[k * C + c];
-  dev::primitives(U, V);
-  const double a = sqrt(1.4 * 287.05 * V[4]);
-  double sum = 0.0;
-  for (int s = 0; s < dev::kMaxCellFaces; ++s) {
-    const int code = t.csr_grad[s * C + c];
-    if (code < 0) continue;
-    const int f = code >> 1;
-    const double un = V[1] * g.fn[f] + V[2] * g.fn[F + f] + V[3] * g.fn[2 * F + f];
-    sum += fabs(un) + a * g.fnn[f];
-  }
-  const double r = t.vol[c] / sum;
-  if (r > 0.0) atomicMin(out, static_cast<unsigned long long>(__double_as_longlong(r)));
 }
 
 }  // namespace
@@ -498,8 +487,7 @@ extern "C" ma_status ma_solver_set_state(ma_solver* s, const double* U, int32_t 
   const dev::TopoView& t = s->mesh->topo;
   if (s->opts.cfl > 0.0) {
     MA_CUDA_TRY(cudaMemsetAsync(s->dscratch, 0xff, sizeof(unsigned long long), s->stream));
-    k_cfl<<<(t.C + 255) / 256, 256, 0, s->stream>>>(t, s->mesh->g64, s->st.Un, s->dscratch);
-    MA_CUDA_TRY(cudaGetLastError());
+    MA_CUDA_TRY(dev::launch_cfl(t, s->mesh->g64, s->st.Un, s->dscratch, s->stream));
     unsigned long long bits = 0;
     MA_CUDA_TRY(cudaMemcpyAsync(&bits, s->dscratch, sizeof(bits), cudaMemcpyDeviceToHost, s->stream));
     MA_CUDA_TRY(cudaStreamSynchronize(s->stream));

@@ -1,0 +1,114 @@
+"""Batched multi-mesh solver on the GPU: each member must equal the same
+solve run alone (bit for bit, both precisions), through membership changes,
+launch-shape changes and the autotuner."""
+import numpy as np
+import pytest
+
+import miniaero_gb300 as ma
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def sod_options(precision=ma.MA_PREC_FP64, second=1, viscous=1):
+    return ma.Options(problem_type=0, lx=1.0, ly=0.5, lz=0.5, second_order_space=second, viscous=viscous,
+                      viscosity_model=ma.MA_VISC_CONSTANT, mu=1.8e-5, prandtl=0.72, ic=ma.MA_IC_SOD, cfl=0.5,
+                      precision=precision)
+
+
+def member(o, dims, ratio_rho, ratio_p):
+    m = o.copy()
+    m.nx, m.ny, m.nz = dims
+    m.sod_left = [0.125 * ratio_rho, 0.1 * ratio_p]
+    md = ma.Parallel3DMesh.from_options(m).fill_mesh_data()
+    return m, md, ma.initial_state(md, m)
+
+
+def single(md, m, U0, steps, dt):
+    s = ma.TimeSolverExplicitRK4(md, m)
+    s.set_state(U0)
+    s.dt = dt
+    s.step(steps)
+    s.synchronize()
+    U = s.get_state()
+    s.close()
+    return U
+
+
+@pytest.mark.parametrize("precision", [ma.MA_PREC_FP64, ma.MA_PREC_MIXED])
+def test_batch_members_equal_single_solves(has_gpu, precision):
+    o = sod_options(precision)
+    dims = [(12, 6, 4), (20, 3, 5), (7, 7, 7), (16, 8, 2), (1, 1, 1)]
+    rng = np.random.default_rng(0)
+    cases = [member(o, d, rng.uniform(2, 20), rng.uniform(2, 20)) for d in dims]
+    b = ma.Batch(o, capacity=16, budget_bytes=1 << 30)
+    ids = []
+    meshes = []
+    for m, md, U0 in cases:
+        dm = ma.DeviceMesh(md)
+        meshes.append(dm)
+        ids.append(b.add(dm, U0))
+    b.step(6)
+    b.synchronize()
+    for (m, md, U0), i in zip(cases, ids):
+        ref = single(md, m, U0, 6, b.member_dt(i))
+        assert np.array_equal(b.get_state(i), ref)
+        if precision == ma.MA_PREC_FP64:
+            assert np.array_equal(ref, oracle.solve(md, m, U0, nsteps=6, dt=b.member_dt(i)))
+    b.close()
+
+
+def test_batch_membership_changes_and_launch_shapes(has_gpu):
+    o = sod_options()
+    rng = np.random.default_rng(1)
+    cases = [member(o, d, rng.uniform(2, 20), rng.uniform(2, 20)) for d in [(10, 4, 4), (6, 6, 6), (14, 2, 3)]]
+    b = ma.Batch(o, capacity=8, budget_bytes=1 << 30)
+    dms = [ma.DeviceMesh(md) for _, md, _ in cases]
+    a = b.add(dms[0], cases[0][2])
+    c = b.add(dms[1], cases[1][2])
+    b.step(3)
+    b.remove(c)                         # leaves mid-run
+    d = b.add(dms[2], cases[2][2])      # joins mid-run
+    b.set_launch([64, 256, 32, 128], [152, 304, 7, 1000])
+    b.step(4)
+    b.synchronize()
+    assert b.member_steps(a) == 7 and b.member_steps(d) == 4
+    m0, md0, U00 = cases[0]
+    assert np.array_equal(b.get_state(a), single(md0, m0, U00, 7, b.member_dt(a)))
+    m2, md2, U02 = cases[2]
+    assert np.array_equal(b.get_state(d), single(md2, m2, U02, 4, b.member_dt(d)))
+    with pytest.raises(ma.MiniaeroError):
+        b.get_state(c)
+    b.close()
+
+
+def test_batch_autotune_preserves_results(has_gpu):
+    o = sod_options()
+    rng = np.random.default_rng(2)
+    cases = [member(o, d, rng.uniform(2, 20), rng.uniform(2, 20)) for d in [(24, 12, 8), (16, 16, 16)]]
+    b = ma.Batch(o, capacity=4, budget_bytes=1 << 30)
+    ids = [b.add(ma.DeviceMesh(md), U0) for _, md, U0 in cases]
+    best = b.autotune(reps=2)
+    assert np.all(best > 0)
+    b.step(5)
+    b.synchronize()
+    for (m, md, U0), i in zip(cases, ids):
+        assert np.array_equal(b.get_state(i), single(md, m, U0, 5, b.member_dt(i)))
+    b.close()
+
+
+def test_batch_budget_is_enforced(has_gpu):
+    o = sod_options()
+    m, md, U0 = member(o, (16, 16, 16), 8.0, 10.0)
+    dm = ma.DeviceMesh(md)
+    probe = ma.Batch(o, capacity=4, budget_bytes=1 << 30)
+    need = probe.member_bytes(dm)
+    probe.close()
+    b = ma.Batch(o, capacity=4, budget_bytes=2 * need + need // 2)
+    b.add(dm, U0)
+    b.add(dm, U0)
+    with pytest.raises(ma.MiniaeroError) as e:
+        b.add(dm, U0)
+    assert e.value.status == 4  # MA_EBUDGET
+    assert b.size == 2 and b.device_bytes == 2 * need
+    b.close()

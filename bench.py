@@ -365,6 +365,14 @@ def run_ours(args, world, rank, local):
         import oracle
         cpu = cpu_baseline_sample(ma, oracle, md, o, U0, dt)
     solver.close()
+    esolver = None
+    dmesh.close()
+    del md
+
+    batched = serving = None
+    if not args.no_extras:
+        batched = run_batched(ma, steps=max(2, min(args.steps, 10)), warmup=args.warmup)
+        serving = run_serving(ma, n_requests=args.serve_requests)
 
     if rank == 0:
         line = {
@@ -387,8 +395,131 @@ def run_ours(args, world, rank, local):
                       "error_after_steps": int(steps_fp64),
                       "kernels": {k: {"ms_per_launch": v[0] / v[1], "launches": v[1]} for k, v in mprof.items()}},
             "cpu_baseline": cpu,
+            "batched": batched,
+            "serving": serving,
         }
         print(json.dumps(line), flush=True)
+
+
+def ensemble_members(ma, n=64, seed=0, lo=16, hi=96):
+    """Batched-ensemble workload: n Sod boxes on 1.0x0.5x0.5, per-axis cell
+    counts log-uniform in [lo, hi], left/right density and pressure ratios
+    uniform in [2, 20] over rho = 0.125, p = 0.1 (seeded)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        dims = [int(round(np.exp(rng.uniform(np.log(lo), np.log(hi))))) for _ in range(3)]
+        rr, pr = rng.uniform(2.0, 20.0, 2)
+        o = ma.Options(problem_type=0, lx=1.0, ly=0.5, lz=0.5, nx=dims[0], ny=dims[1], nz=dims[2],
+                       second_order_space=1, viscous=1, viscosity_model=1, mu=1.8e-5, prandtl=0.72, ic=1,
+                       sod_left=[0.125 * rr, 0.1 * pr], sod_right=[0.125, 0.1], cfl=0.5)
+        out.append(o)
+    return out
+
+
+def run_batched(ma, steps, warmup, n_members=64):
+    """64 meshes in one batch, FP64 and mixed, autotuned launch shapes."""
+    import torch
+    members = ensemble_members(ma, n_members)
+    t0 = time.perf_counter()
+    built = []
+    for o in members:
+        md = ma.Parallel3DMesh.from_options(o).fill_mesh_data()
+        built.append((o, md, ma.initial_state(md, o), ma.DeviceMesh(md)))
+    setup_s = time.perf_counter() - t0
+    cells = sum(b[1].ncells for b in built)
+    res = {"workload": "64 Sod boxes, per-axis cells log-uniform [16, 96] (seed 0), 2nd order viscous, CFL 0.5",
+           "meshes": n_members, "cells": cells, "host_setup_s": setup_s, "timed_steps": steps}
+    for prec_name, prec in (("fp64", ma.MA_PREC_FP64), ("mixed", ma.MA_PREC_MIXED)):
+        phys = members[0].copy()
+        phys.precision = prec
+        b = ma.Batch(phys, capacity=n_members, budget_bytes=200 << 30)
+        ids = [b.add(dm, U0) for (o, md, U0, dm) in built]
+        tuned = b.autotune(reps=2)
+        b.step(warmup)
+        b.synchronize()
+        stream = torch.cuda.ExternalStream(b.stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        b.step(steps)
+        e1.record(stream)
+        b.synchronize()
+        ms = e0.elapsed_time(e1)
+        # Same members one after another through the single-mesh solver.
+        seq_ms = 0.0
+        for (o, md, U0, dm) in built:
+            so = o.copy()
+            so.precision = prec
+            s = ma.TimeSolverExplicitRK4(md, so, device_mesh=dm)
+            s.set_state(U0)
+            s.step(1)
+            s.synchronize()
+            st = torch.cuda.ExternalStream(s.stream)
+            a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a0.record(st)
+            s.step(steps)
+            a1.record(st)
+            s.synchronize()
+            seq_ms += a0.elapsed_time(a1)
+            s.close()
+        block, grid = b.launch
+        res[prec_name] = {"value": cells * 4 * steps / (ms / 1e3) / 1e6, "unit": "Mcell-stage/s",
+                          "ms_per_step": ms / steps,
+                          "sequential_single_mesh_value": cells * 4 * steps / (seq_ms / 1e3) / 1e6,
+                          "autotuned": {"block": block, "grid": grid, "ms_per_launch": tuned.tolist()},
+                          "launches_per_step": 16}
+        b.close()
+    return res
+
+
+def run_serving(ma, n_requests=32, rate=200.0, nsteps=500, seed=1, budget=150 << 30, tick=25):
+    """Serving stream: Poisson arrivals (rate/s, seeded) of flat-plate solves,
+    Mach uniform in [0.1, 0.6], sizes from {32,48,64,96,128}^3, nsteps RK4
+    steps each, mixed precision, admitted under the HBM budget."""
+    rng = np.random.default_rng(seed)
+    sizes = [32, 48, 64, 96, 128]
+    phys = ma.Options(problem_type=1, second_order_space=1, viscous=1, limiter=ma.MA_LIMITER_VANALBADA,
+                      viscosity_model=ma.MA_VISC_CONSTANT, mu=1.8e-5, prandtl=0.72, precision=ma.MA_PREC_MIXED,
+                      cfl=0.5)
+    srv = ma.Server(phys, budget_bytes=budget, tick_steps=tick, capacity=512, thread=True)
+    t0 = time.perf_counter()
+    for n in sizes:  # mesh cache warm-up: one device mesh per size
+        srv.preload(ma.Server.request(n, n, n, 2.0, 0.5, 0.5, flat_plate_inflow(0.3), nsteps))
+    setup_s = time.perf_counter() - t0
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_requests))
+    reqs = [(float(a), int(rng.choice(sizes)), float(rng.uniform(0.1, 0.6))) for a in arrivals]
+    ids = []
+    start = time.perf_counter()
+    for at, n, mach in reqs:
+        now = time.perf_counter() - start
+        if at > now:
+            time.sleep(at - now)
+        ids.append(srv.submit(ma.Server.request(n, n, n, 2.0, 0.5, 0.5, flat_plate_inflow(mach), nsteps)))
+    for rid in ids:
+        srv.wait(rid, timeout=3600.0)
+    wall = time.perf_counter() - start
+    infos = [srv.query(r) for r in ids]
+    st = srv.stats()
+    srv.close()
+    lat = np.array([(i.t_finish_ns - i.t_submit_ns) / 1e9 for i in infos])
+    queue = np.array([(i.t_admit_ns - i.t_submit_ns) / 1e9 for i in infos])
+    done = sum(1 for i in infos if i.state == 2)
+    cell_stages = sum(i.cells * 4 * nsteps for i in infos if i.state == 2)
+    offered = sum(n ** 3 * 4 * nsteps for _, n, _ in reqs) / (reqs[-1][0] if reqs[-1][0] > 0 else 1.0)
+    return {"workload": "Poisson %.0f/s flat-plate requests, Mach U[0.1,0.6], sizes {32..128}^3, %d steps, mixed"
+                        % (rate, nsteps),
+            "requests": n_requests, "completed": done, "tick_steps": tick, "budget_bytes": budget,
+            "mesh_cache_setup_s": setup_s,
+            "throughput": {"value": cell_stages / wall / 1e6, "unit": "Mcell-stage/s (wall, first arrival to last)"},
+            "throughput_busy": {"value": st["cell_stages"] / max(st["busy_seconds"], 1e-9) / 1e6,
+                                "unit": "Mcell-stage/s (while requests run)"},
+            "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                          "max": float(lat.max())},
+            "queue_wait_s": {"p50": float(np.percentile(queue, 50)), "p99": float(np.percentile(queue, 99))},
+            "peak_running": st["peak_running"], "peak_bytes": st["peak_bytes"],
+            "offered_load_mcell_stage_s": offered / 1e6,
+            "saturated": bool(offered / 1e6 > cell_stages / wall / 1e6)}
 
 
 def main():
@@ -399,6 +530,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched and serving sections")
+    ap.add_argument("--serve-requests", type=int, default=32)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

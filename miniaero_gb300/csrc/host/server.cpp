@@ -101,17 +101,20 @@ struct ma_server {
 
 namespace {
 
+// Device bytes of a request's member state and of its mesh, from the mesh
+// dimensions. They bound the allocations of ma_batch_add / ma_mesh_upload
+// from above (array padding included), so admission never overshoots.
 size_t dry_member_bytes(const ma_server* s, const ma_request& r) {
   int64_t C, F;
   box_counts(r, C, F);
   const size_t w = s->physics.precision == MA_PREC_MIXED ? 4 : 8;
-  return static_cast<size_t>(C) * (80 + 25 * w) + static_cast<size_t>(F) * 5 * w;
+  return static_cast<size_t>(C) * (80 + 25 * w) + static_cast<size_t>(F) * 5 * w + 6 * 256;
 }
 
 size_t dry_mesh_bytes(const ma_request& r) {
   int64_t C, F;
   box_counts(r, C, F);
-  return static_cast<size_t>(C) * 100 + static_cast<size_t>(F) * 236;
+  return static_cast<size_t>(C) * 100 + static_cast<size_t>(F) * 236 + 16 * 256;
 }
 
 MeshKey key_of(const ma_request& r) {
@@ -203,11 +206,9 @@ void admit(ma_server* s) {
     }
     if (s->stats.running >= s->stats.capacity) return;
     const bool cached = s->meshes.count(q.key) != 0;
-    const size_t mesh_need = cached ? 0 : (s->dry ? dry_mesh_bytes(q.req) : 0);
-    size_t member_need = s->dry ? dry_member_bytes(s, q.req) : 0;
-    if (s->dry) {
-      if (!make_room(s, mesh_need + member_need)) return;  // wait for memory
-    }
+    const size_t mesh_need = cached ? 0 : dry_mesh_bytes(q.req);
+    size_t member_need = dry_member_bytes(s, q.req);
+    if (!make_room(s, mesh_need + member_need)) return;  // wait for memory
     CachedMesh* cm = nullptr;
     ma_status st = ensure_mesh(s, q, &cm);
     if (st != MA_OK) {
@@ -221,10 +222,6 @@ void admit(ma_server* s) {
     cm->last_used = ns_since(s->t0);
     if (!s->dry) {
       member_need = ma_batch_member_bytes(s->batch, cm->dev);
-      if (!make_room(s, member_need)) {
-        cm->users--;
-        return;
-      }
       const ma_options o = options_of(s, q.req);
       int64_t C, F;
       box_counts(q.req, C, F);
@@ -407,7 +404,7 @@ extern "C" ma_status ma_server_submit(ma_server* s, const ma_request* r, int64_t
   q.key = key_of(*r);
   q.t_submit = ns_since(s->t0);
   // A request that cannot fit even in an empty server is rejected now.
-  if (s->dry && dry_member_bytes(s, *r) + dry_mesh_bytes(*r) > s->budget) {
+  if (dry_member_bytes(s, *r) + dry_mesh_bytes(*r) > s->budget) {
     q.state = MA_REQ_FAILED;
     q.error = MA_EBUDGET;
     q.message = "request larger than the device-memory budget";
@@ -430,7 +427,7 @@ extern "C" ma_status ma_server_preload_mesh(ma_server* s, const ma_request* r) {
   q.req = *r;
   q.key = key_of(*r);
   CachedMesh* cm = nullptr;
-  const size_t need = s->meshes.count(q.key) ? 0 : (s->dry ? dry_mesh_bytes(*r) : 0);
+  const size_t need = s->meshes.count(q.key) ? 0 : dry_mesh_bytes(*r);
   if (need && !make_room(s, need)) return set_error(MA_EBUDGET, "mesh does not fit the budget");
   ma_status st = ensure_mesh(s, q, &cm);
   if (st == MA_OK) cm->last_used = ns_since(s->t0);

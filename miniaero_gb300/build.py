@@ -30,7 +30,7 @@ HOST_CXX = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall"]
 # (source, extra flags)
 DEVICE_SOURCES = [
     ("device/kernels_fp64.cu", ["--fmad=false"]),
-    ("device/kernels_mixed.cu", ["--fmad=true"]),
+    ("device/kernels_mixed.cu", ["--fmad=false"]),
     ("device/ops.cu", ["--fmad=false"]),
     ("device/solver.cu", ["--fmad=false"]),
     ("device/batch.cu", ["--fmad=false"]),

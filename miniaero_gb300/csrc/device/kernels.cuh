@@ -24,6 +24,9 @@ struct TopoView {
   const int32_t* csr_grad = nullptr;   // Green-Gauss / min-max / limiter order
   const int32_t* csr_nbr = nullptr;    // neighbour cell of each csr_grad slot (-1 boundary)
   const int32_t* csr_flux = nullptr;   // residual order
+  // 1 where the cell is axis-aligned and its csr_grad list is grouped by axis
+  // (two faces each for x, y, z): gradient terms along other axes are zero.
+  const uint8_t* axis_cell = nullptr;
 };
 
 // Geometry in the arithmetic type R of the flux/gradient/limiter work.

@@ -89,6 +89,49 @@ __device__ __forceinline__ void sweep1_cell(const TopoView& t, const GeomView<R>
     mn[k] = big_value<R>();
     mx[k] = -big_value<R>();
   }
+  if (t.axis_cell[c]) {
+    // Axis-aligned cell: slots 2p, 2p+1 are its faces normal to axis p, in
+    // serial order; only gradient components along p get nonzero terms.
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+#pragma unroll 1
+      for (int q = 0; q < 2; ++q) {
+        const int s = 2 * p + q;
+        const int code = t.csr_grad[s * C + c];
+        const int f = code >> 1;
+        const bool left = code & 1;
+        const R np = g.fn[p * F + f];
+        if (f < t.Fi) {
+          const int nb = t.csr_nbr[s * C + c];
+          R wn[5];
+#pragma unroll
+          for (int k = 0; k < 5; ++k) wn[k] = W[k * C + nb];
+#pragma unroll
+          for (int k = 0; k < 5; ++k) {
+            const R pl = left ? wc[k] : wn[k];
+            const R pr = left ? wn[k] : wc[k];
+            const R gr = R(0.5) * (pl + pr) * np;
+            acc[k][p] += left ? div_by_recip(gr, V, Vinv) : div_by_recip(-gr, V, Vinv);
+            if (MODE > 0) {
+              const R fmin_ = (pr < pl) ? pr : pl;
+              const R fmax_ = (pr > pl) ? pr : pl;
+              mn[k] = (fmin_ < mn[k]) ? fmin_ : mn[k];
+              mx[k] = (mx[k] < fmax_) ? fmax_ : mx[k];
+            }
+          }
+        } else {
+#pragma unroll
+          for (int k = 0; k < 5; ++k) {
+            acc[k][p] += div_by_recip(wc[k] * np, V, Vinv);
+            if (MODE > 0) {
+              mn[k] = (wc[k] < mn[k]) ? wc[k] : mn[k];
+              mx[k] = (mx[k] < wc[k]) ? wc[k] : mx[k];
+            }
+          }
+        }
+      }
+    }
+  } else {
   // Gradient contributions and min/max, in the reference's serial face order.
 #pragma unroll 1
   for (int s = 0; s < kMaxCellFaces; ++s) {
@@ -130,6 +173,7 @@ __device__ __forceinline__ void sweep1_cell(const TopoView& t, const GeomView<R>
         }
       }
     }
+  }
   }
   R gsum[5][3];
 #pragma unroll

@@ -1,5 +1,7 @@
 // Mixed form: FP32 face flux, gradient and limiter; FP64 residual
-// accumulation, RK4 update and primitives of the FP64 state.
+// accumulation and RK4 update. Built with --fmad=false like the FP64 form:
+// without contraction every item's arithmetic is the same in the single-mesh
+// and the batched kernels, so a solve gives identical bits alone or batched.
 #include "kernels_impl.cuh"
 
 namespace miniaero {

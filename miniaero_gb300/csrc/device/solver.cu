@@ -239,6 +239,43 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
             push(csr_flux, nf, v->bc[b].conn[2 * i], ((bc_base[b] + i) << 1) | 1, 0, false);
     if (overflow) return set_error(MA_EINVAL, "a cell has more than 6 faces");
 
+    // Axis-aligned cells: every face area vector has exactly one nonzero
+    // component and each axis owns two faces. A gradient component (k, d)
+    // then receives nonzero terms only from the two d-faces; the other terms
+    // are signed zeros, which cannot change an accumulator that starts at +0.
+    // The gradient list of such a cell is regrouped by axis (x, x, y, y, z, z),
+    // keeping the serial order within each axis, and the cell is flagged.
+    std::vector<uint8_t> axis_cell(C, 0);
+    {
+      auto axis_of = [&](int32_t g) -> int {
+        int nz = 0, ax = -1;
+        for (int d = 0; d < 3; ++d)
+          if (geo[d * static_cast<size_t>(F) + g] != 0.0) { ++nz; ax = d; }
+        return nz == 1 ? ax : -1;
+      };
+      for (int32_t c = 0; c < C; ++c) {
+        if (ng[c] != K) continue;
+        int32_t codes[6], nbrs[6], axes[6], count[3] = {0, 0, 0};
+        bool ok = true;
+        for (size_t s2 = 0; s2 < K && ok; ++s2) {
+          codes[s2] = csr_grad[s2 * C + c];
+          nbrs[s2] = csr_nbr[s2 * C + c];
+          axes[s2] = axis_of(codes[s2] >> 1);
+          if (axes[s2] < 0 || ++count[axes[s2]] > 2) ok = false;
+        }
+        if (!ok) continue;
+        size_t out = 0;
+        for (int d = 0; d < 3; ++d)
+          for (size_t s2 = 0; s2 < K; ++s2)
+            if (axes[s2] == d) {
+              csr_grad[out * C + c] = codes[s2];
+              csr_nbr[out * C + c] = nbrs[s2];
+              ++out;
+            }
+        axis_cell[c] = 1;
+      }
+    }
+
     // Device arena.
     Arena a;
     auto layout = [&](ma_mesh& m) {
@@ -247,6 +284,7 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
       m.topo.csr_grad = a.take<int32_t>(K * C);
       m.topo.csr_nbr = a.take<int32_t>(K * C);
       m.topo.csr_flux = a.take<int32_t>(K * C);
+      m.topo.axis_cell = a.take<uint8_t>(C);
       double* g64 = a.take<double>(19 * static_cast<size_t>(F));
       float* g32 = a.take<float>(19 * static_cast<size_t>(F));
       double* vol64 = const_cast<double*>(m.topo.vol);
@@ -302,6 +340,7 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
     if (e == cudaSuccess) e = copy(m->topo.csr_grad, csr_grad.data(), sizeof(int32_t) * csr_grad.size());
     if (e == cudaSuccess) e = copy(m->topo.csr_nbr, csr_nbr.data(), sizeof(int32_t) * csr_nbr.size());
     if (e == cudaSuccess) e = copy(m->topo.csr_flux, csr_flux.data(), sizeof(int32_t) * csr_flux.size());
+    if (e == cudaSuccess) e = copy(m->topo.axis_cell, axis_cell.data(), axis_cell.size());
     if (e == cudaSuccess) e = copy(m->g64.fn, geo.data(), sizeof(double) * geo.size());
     if (e == cudaSuccess) e = copy(m->g32.fn, geo32.data(), sizeof(float) * geo32.size());
     if (e == cudaSuccess) e = copy(m->g32.vol, vol32.data(), sizeof(float) * vol32.size());

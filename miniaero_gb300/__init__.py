@@ -345,7 +345,9 @@ class Batch:
         self._meshes.pop(member_id, None)
 
     def get_state(self, member_id):
-        dm = self._meshes[member_id]
+        dm = self._meshes.get(member_id)
+        if dm is None:
+            raise MiniaeroError(_lib.MA_ENOTFOUND, "unknown batch member %r" % member_id)
         U = np.empty((dm.ncells, 5), np.float64)
         check(lib().ma_batch_get_state(self._h, int(member_id), f64p(U), MA_LAYOUT_AOS))
         return U

@@ -16,6 +16,9 @@ constexpr int kMaxCellFaces = 6;  // Hexa8: every face is internal or boundary
 struct TopoView {
   int32_t C = 0, Fi = 0, Fb = 0, F = 0;
   int32_t nbc_type[4] = {0, 0, 0, 0};  // BC face counts in type order E, T, N, I
+  // Internal faces [0, fi_axis_end[0]) have frames aligned with x, then y up
+  // to fi_axis_end[1], then z up to fi_axis_end[2]; the rest are general.
+  int32_t fi_axis_end[3] = {0, 0, 0};
   const double* vol = nullptr;         // [C]
   const double* vinv = nullptr;        // [C] 1/V rounded to nearest
   const int32_t* fconn = nullptr;      // [2][F] (left, right); right = -1 on a boundary

@@ -246,6 +246,29 @@ __device__ __forceinline__ void sweep1_cell(const TopoView& t, const GeomView<R>
   }
 }
 
+// Roe (+ viscous) flux of an internal face whose frame is aligned with axis D.
+template <class R, bool VISC, int D>
+__device__ __forceinline__ void face_flux_axis(const TopoView& t, const GeomView<R>& g, const R* __restrict__ grad,
+                                               const R pl[5], const R pr[5], const Transport& tr, int f, int L,
+                                               int Rc, R flux[5]) {
+  constexpr int T = (D + 2) % 3, B = (D + 1) % 3;
+  const int C = t.C, F = t.F;
+  const R nD = g.fn[D * F + f];
+  roe_flux_axis<R, D>(pl, pr, nD, g.fnu[D * F + f], g.ftu[T * F + f], g.fbu[B * F + f], g.fnn[f], flux);
+  if (VISC) {
+    R pf[5], gf[5][3], vf[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      pf[k] = R(0.5) * (pl[k] + pr[k]);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) gf[k][d] = R(0.5) * (grad[(3 * k + d) * C + L] + grad[(3 * k + d) * C + Rc]);
+    }
+    viscous_flux_axis<R, D>(gf, pf, nD, tr, vf);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) flux[k] -= vf[k];
+  }
+}
+
 template <class R, bool SECOND, bool VISC>
 __device__ __forceinline__ void internal_flux_face(const TopoView& t, const GeomView<R>& g, const R* __restrict__ W,
                                                    const R* __restrict__ grad, const R* __restrict__ phi,
@@ -274,20 +297,28 @@ __device__ __forceinline__ void internal_flux_face(const TopoView& t, const Geom
       pr[k] += trr * phi[k * C + Rc];
     }
   }
-  const FaceFrame<R> fr = load_frame<R>(g, f, F);
   R flux[5];
-  roe_flux<R>(pl, pr, fr, flux);
-  if (VISC) {
-    R pf[5], gf[5][3], vf[5];
+  // Faces [0, axis_end[2]) are axis-aligned, grouped by the axis of their
+  // area vector; the rest take the general path.
+  const int axis = f < t.fi_axis_end[0] ? 0 : f < t.fi_axis_end[1] ? 1 : f < t.fi_axis_end[2] ? 2 : 3;
+  if (axis == 0) face_flux_axis<R, VISC, 0>(t, g, grad, pl, pr, tr, f, L, Rc, flux);
+  else if (axis == 1) face_flux_axis<R, VISC, 1>(t, g, grad, pl, pr, tr, f, L, Rc, flux);
+  else if (axis == 2) face_flux_axis<R, VISC, 2>(t, g, grad, pl, pr, tr, f, L, Rc, flux);
+  else {
+    const FaceFrame<R> fr = load_frame<R>(g, f, F);
+    roe_flux<R>(pl, pr, fr, flux);
+    if (VISC) {
+      R pf[5], gf[5][3], vf[5];
 #pragma unroll
-    for (int k = 0; k < 5; ++k) {
-      pf[k] = R(0.5) * (pl[k] + pr[k]);
+      for (int k = 0; k < 5; ++k) {
+        pf[k] = R(0.5) * (pl[k] + pr[k]);
 #pragma unroll
-      for (int d = 0; d < 3; ++d) gf[k][d] = R(0.5) * (grad[(3 * k + d) * C + L] + grad[(3 * k + d) * C + Rc]);
+        for (int d = 0; d < 3; ++d) gf[k][d] = R(0.5) * (grad[(3 * k + d) * C + L] + grad[(3 * k + d) * C + Rc]);
+      }
+      viscous_flux<R>(gf, pf, fr.n, tr, vf);
+#pragma unroll
+      for (int k = 0; k < 5; ++k) flux[k] -= vf[k];
     }
-    viscous_flux<R>(gf, pf, fr.n, tr, vf);
-#pragma unroll
-    for (int k = 0; k < 5; ++k) flux[k] -= vf[k];
   }
 #pragma unroll
   for (int k = 0; k < 5; ++k) fflux[static_cast<size_t>(f) * 5 + k] = flux[k];

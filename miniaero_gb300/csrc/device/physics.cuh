@@ -167,6 +167,153 @@ __device__ __forceinline__ void roe_flux(const R pl[5], const R pr[5], const Fac
   }
 }
 
+// Roe flux on an axis-aligned face: the area vector and unit normal are
+// nonzero only along axis D, the unit tangent only along T = (D+2)%3 and the
+// unit binormal only along B = (D+1)%3 (the frame the mesh builds for such a
+// face; the host checks the zero pattern). Every product with one of the
+// exactly-zero components is a signed zero; the terms left are evaluated in
+// the reference's order, so every nonzero intermediate equals roe_flux's. A
+// zero intermediate may differ in sign only; none reaches a division, a
+// square root or a comparison that could tell.
+template <class R, int D>
+__device__ __forceinline__ void roe_flux_axis(const R pl[5], const R pr[5], R nD, R nuD, R tuT, R buB, R nn,
+                                              R flux[5]) {
+  constexpr int T = (D + 2) % 3, B = (D + 1) % 3;
+  const R efix_u = R(0.1), efix_c = R(0.1), gm1 = R(0.4);
+  const R rl = pl[0];
+  const R vel_l[3] = {pl[1], pl[2], pl[3]};
+  const R p_l = rl * R(287.05) * pl[4];
+  const R h_l = R(1004.0) * pl[4];
+  const R H_l = h_l + R(0.5) * (vel_l[0] * vel_l[0] + vel_l[1] * vel_l[1] + vel_l[2] * vel_l[2]);
+  const R mf_l = rl * (nD * vel_l[D]);
+  const R rr = pr[0];
+  const R vel_r[3] = {pr[1], pr[2], pr[3]};
+  const R p_r = rr * R(287.05) * pr[4];
+  const R h_r = R(1004.0) * pr[4];
+  const R H_r = h_r + R(0.5) * (vel_r[0] * vel_r[0] + vel_r[1] * vel_r[1] + vel_r[2] * vel_r[2]);
+  const R mf_r = rr * (nD * vel_r[D]);
+  const R psum = p_l + p_r;
+
+  flux[0] = R(0.5) * (mf_l + mf_r);
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+    flux[1 + j] = (j == D) ? R(0.5) * (mf_l * vel_l[j] + mf_r * vel_r[j] + nD * psum)
+                           : R(0.5) * (mf_l * vel_l[j] + mf_r * vel_r[j]);
+  flux[4] = R(0.5) * (mf_l * H_l + mf_r * H_r);
+
+  const R srl = dsqrt<R>(rl);
+  const R denom = R(1.0) / (srl + dsqrt<R>(rr));
+  const R alpha = srl * denom;
+  const R beta = R(1.0) - alpha;
+  R vroe[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) vroe[j] = alpha * vel_l[j] + beta * vel_r[j];
+  const R hroe = alpha * h_l + beta * h_r +
+                 R(0.5) * alpha * beta *
+                     ((vel_r[0] - vel_l[0]) * (vel_r[0] - vel_l[0]) + (vel_r[1] - vel_l[1]) * (vel_r[1] - vel_l[1]) +
+                      (vel_r[2] - vel_l[2]) * (vel_r[2] - vel_l[2]));
+  const R c = dsqrt<R>(gm1 * hroe);
+
+  const R nv = vroe[D] * nuD;
+  const R tv = vroe[T] * tuT;
+  const R bv = vroe[B] * buB;
+  const R ke = R(0.5) * (vroe[0] * vroe[0] + vroe[1] * vroe[1] + vroe[2] * vroe[2]);
+  const R cssi = R(1.0) / (c * c);
+  const R hcssi = R(0.5) * cssi;
+
+  R dq[5];
+  dq[0] = rr - rl;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) dq[1 + j] = rr * vel_r[j] - rl * vel_l[j];
+  dq[4] = (rr * H_r - p_r) - (rl * H_l - p_l);
+
+  const R cbar = c * nn;
+  const R ubar = vroe[D] * nD;
+  const R cfl = dabs<R>(ubar) + cbar;
+  const R eig1 = ubar + cbar, eig2 = ubar - cbar, eig3 = ubar;
+  R a1 = dabs<R>(eig1), a2 = dabs<R>(eig2), a3 = dabs<R>(eig3);
+  const R epuc = efix_u * cfl, epcc = efix_c * cfl;
+  if (a1 < epcc) a1 = R(0.5) * (eig1 * eig1 + epcc * epcc) / epcc;
+  if (a2 < epcc) a2 = R(0.5) * (eig2 * eig2 + epcc * epcc) / epcc;
+  if (a3 < epuc) a3 = R(0.5) * (eig3 * eig3 + epuc * epuc) / epuc;
+  const R ep1 = R(0.5) * (eig1 + a1), em1 = R(0.5) * (eig1 - a1);
+  const R ep2 = R(0.5) * (eig2 + a2), em2 = R(0.5) * (eig2 - a2);
+  const R ep3 = R(0.5) * (eig3 + a3), em3 = R(0.5) * (eig3 - a3);
+  const R lam[5] = {ep1 - em1, ep2 - em2, ep3 - em3, ep3 - em3, ep3 - em3};
+
+  // Left eigenvectors: rows 0/1 hold c*nu_j - gm1*u_j (c*nu_j = +-0 off D),
+  // rows 3/4 have a single nonzero tangent/binormal entry.
+  const R gk = gm1 * (ke - hroe);
+  R row0[5], row1[5];
+  row0[0] = gk + c * (c - nv);
+  row1[0] = gk + c * (c + nv);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    row0[1 + j] = (j == D) ? c * nuD - gm1 * vroe[j] : -(gm1 * vroe[j]);
+    row1[1 + j] = (j == D) ? -c * nuD - gm1 * vroe[j] : -(gm1 * vroe[j]);
+  }
+  row0[4] = gm1;
+  row1[4] = gm1;
+  R ldq[5];
+  {
+    R a0 = R(0.0), b0 = R(0.0), c0 = R(0.0);
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+      a0 += row0[j] * dq[j];
+      b0 += row1[j] * dq[j];
+    }
+    c0 += (ke - hroe) * dq[0];
+    c0 += -vroe[0] * dq[1];
+    c0 += -vroe[1] * dq[2];
+    c0 += -vroe[2] * dq[3];
+    c0 += R(1.0) * dq[4];
+    R d0 = R(0.0);
+    d0 += -tv * dq[0];
+    d0 += tuT * dq[1 + T];
+    R e0 = R(0.0);
+    e0 += -bv * dq[0];
+    e0 += buB * dq[1 + B];
+    ldq[0] = lam[0] * a0;
+    ldq[1] = lam[1] * b0;
+    ldq[2] = lam[2] * c0;
+    ldq[3] = lam[3] * d0;
+    ldq[4] = lam[4] * e0;
+  }
+  // Right eigenvectors.
+  const R hk = hroe + ke;
+  {
+    R acc = R(0.0);
+    acc += hcssi * ldq[0];
+    acc += hcssi * ldq[1];
+    acc += -gm1 * cssi * ldq[2];
+    flux[0] -= R(0.5) * acc;
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    R acc = R(0.0);
+    if (j == D) {
+      acc += (vroe[j] + nuD * c) * hcssi * ldq[0];
+      acc += (vroe[j] - nuD * c) * hcssi * ldq[1];
+    } else {
+      acc += vroe[j] * hcssi * ldq[0];
+      acc += vroe[j] * hcssi * ldq[1];
+    }
+    acc += -gm1 * vroe[j] * cssi * ldq[2];
+    if (j == T) acc += tuT * ldq[3];
+    if (j == B) acc += buB * ldq[4];
+    flux[1 + j] -= R(0.5) * acc;
+  }
+  {
+    R acc = R(0.0);
+    acc += (hk + c * nv) * hcssi * ldq[0];
+    acc += (hk - c * nv) * hcssi * ldq[1];
+    acc += (c * c - gm1 * hk) * cssi * ldq[2];
+    acc += tv * ldq[3];
+    acc += bv * ldq[4];
+    flux[4] -= R(0.5) * acc;
+  }
+}
+
 // Gas transport: Sutherland law (reference) or constant mu with given Prandtl.
 struct Transport {
   int model;       // 0 Sutherland, 1 constant
@@ -218,6 +365,32 @@ __device__ __forceinline__ void viscous_flux(const R g[5][3], const R prim[5], c
     }
     vflux[4] += kc * g[4][i] * a[i];
   }
+}
+
+// viscous_flux for an area vector that is nonzero only along axis D: the
+// terms with a zero area component are signed zeros in +0-started sums.
+template <class R, int D>
+__device__ __forceinline__ void viscous_flux_axis(const R g[5][3], const R prim[5], R aD, const Transport& tr,
+                                                  R vflux[5]) {
+  R mu, kc;
+  transport<R>(tr, prim[4], mu, kc);
+  R div = R(0);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) div += g[i + 1][i];
+  const R div3 = div_by_recip(div * R(1), R(3.), R(1.0 / 3.0));
+  vflux[0] = R(0.0);
+  R v4 = R(0.0);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const R S = R(0.5) * (g[i + 1][D] + g[D + 1][i]);
+    const R tiD = (i == D) ? S - div3 : S;
+    R vi = R(0.0);
+    vi += (R(2) * mu * tiD) * aD;
+    vflux[1 + i] = vi;
+    v4 += (R(2) * mu * tiD) * prim[i + 1] * aD;
+    if (i == D) v4 += kc * g[4][D] * aD;
+  }
+  vflux[4] = v4;
 }
 
 template <class R>

@@ -161,6 +161,39 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
       pass(order, tmp, 0);
       order.swap(tmp);
     }
+    // Axis-aligned faces first, grouped by axis (x, y, z), then the general
+    // ones; (left, right) order within each group. A face is aligned with
+    // axis D when its area vector is nonzero only along D, its tangent only
+    // along (D+2)%3 and its binormal only along (D+1)%3.
+    int32_t axis_end[3] = {0, 0, 0};
+    {
+      auto face_axis = [&](int32_t i) -> int {
+        const double* n = &v->internal.normal[3 * static_cast<size_t>(i)];
+        const double* tt = &v->internal.tangent[3 * static_cast<size_t>(i)];
+        const double* b = &v->internal.binormal[3 * static_cast<size_t>(i)];
+        for (int D = 0; D < 3; ++D) {
+          const int T = (D + 2) % 3, B = (D + 1) % 3;
+          bool ok = n[D] != 0.0 && tt[T] != 0.0 && b[B] != 0.0;
+          for (int d = 0; d < 3 && ok; ++d) {
+            if (d != D && n[d] != 0.0) ok = false;
+            if (d != T && tt[d] != 0.0) ok = false;
+            if (d != B && b[d] != 0.0) ok = false;
+          }
+          if (ok) return D;
+        }
+        return 3;
+      };
+      std::vector<int32_t> grouped;
+      grouped.reserve(Fi);
+      std::vector<uint8_t> cls(Fi);
+      for (int32_t i = 0; i < Fi; ++i) cls[i] = static_cast<uint8_t>(face_axis(i));
+      for (int k = 0; k < 4; ++k) {
+        for (int32_t g = 0; g < Fi; ++g)
+          if (cls[order[g]] == k) grouped.push_back(order[g]);
+        if (k < 3) axis_end[k] = static_cast<int32_t>(grouped.size());
+      }
+      order.swap(grouped);
+    }
     std::vector<int32_t> gpu_of_internal(Fi);
     for (int32_t g = 0; g < Fi; ++g) gpu_of_internal[order[g]] = g;
 
@@ -321,6 +354,7 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
     m->topo.Fb = Fb;
     m->topo.F = F;
     for (int r = 0; r < 4; ++r) m->topo.nbc_type[r] = nbc_type[r];
+    for (int k = 0; k < 3; ++k) m->topo.fi_axis_end[k] = axis_end[k];
 
     std::vector<float> geo32(geo.size());
     for (size_t i = 0; i < geo.size(); ++i) geo32[i] = static_cast<float>(geo[i]);

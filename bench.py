@@ -522,16 +522,19 @@ def run_batched(ma, steps, warmup, n_members=64):
     return res
 
 
-def run_serving(ma, n_requests=32, rate=200.0, nsteps=500, seed=1, budget=150 << 30, tick=25):
+def run_serving(ma, n_requests=32, rate=200.0, nsteps=500, seed=1, budget=150 << 30, tick=25,
+                max_running_cells=8_000_000):
     """Serving stream: Poisson arrivals (rate/s, seeded) of flat-plate solves,
     Mach uniform in [0.1, 0.6], sizes from {32,48,64,96,128}^3, nsteps RK4
-    steps each, mixed precision, admitted under the HBM budget."""
+    steps each, mixed precision, admitted under the HBM budget with at most
+    max_running_cells cells running at once (enough to fill the GPU)."""
     rng = np.random.default_rng(seed)
     sizes = [32, 48, 64, 96, 128]
     phys = ma.Options(problem_type=1, second_order_space=1, viscous=1, limiter=ma.MA_LIMITER_VANALBADA,
                       viscosity_model=ma.MA_VISC_CONSTANT, mu=1.8e-5, prandtl=0.72, precision=ma.MA_PREC_MIXED,
                       cfl=0.5)
     srv = ma.Server(phys, budget_bytes=budget, tick_steps=tick, capacity=512, thread=True)
+    srv.set_max_running_cells(max_running_cells)
     t0 = time.perf_counter()
     for n in sizes:  # mesh cache warm-up: one device mesh per size
         srv.preload(ma.Server.request(n, n, n, 2.0, 0.5, 0.5, flat_plate_inflow(0.3), nsteps))
@@ -559,6 +562,7 @@ def run_serving(ma, n_requests=32, rate=200.0, nsteps=500, seed=1, budget=150 <<
     return {"workload": "Poisson %.0f/s flat-plate requests, Mach U[0.1,0.6], sizes {32..128}^3, %d steps, mixed"
                         % (rate, nsteps),
             "requests": n_requests, "completed": done, "tick_steps": tick, "budget_bytes": budget,
+            "max_running_cells": max_running_cells,
             "mesh_cache_setup_s": setup_s,
             "throughput": {"value": cell_stages / wall / 1e6, "unit": "Mcell-stage/s (wall, first arrival to last)"},
             "throughput_busy": {"value": st["cell_stages"] / max(st["busy_seconds"], 1e-9) / 1e6,

@@ -263,6 +263,9 @@ typedef struct {
 ma_status ma_server_create(const ma_options* physics, size_t budget_bytes, int32_t tick_steps, int32_t capacity,
                            int32_t flags, ma_server** out);
 void ma_server_free(ma_server* s);
+/* Admission cap on the cells of running requests (0 = none; default). A
+ * request larger than the cap still runs when nothing else does. */
+ma_status ma_server_set_max_running_cells(ma_server* s, int64_t cells);
 /* Thread-safe; returns at once with the request id. */
 ma_status ma_server_submit(ma_server* s, const ma_request* r, int64_t* id);
 /* Builds and caches the device mesh a request of this shape would use. */
@@ -288,7 +291,8 @@ ma_status ma_debug_binsort(const int32_t* keys, int32_t n, int32_t* perm);
 
 /* Checks the device's reciprocal-based correctly rounded division against
  * IEEE division on n generated pairs (mode 0 random, 1 divisors with an
- * all-ones significand, 2 quotients near rounding midpoints). Returns the
+ * all-ones significand, 2 quotients near rounding midpoints); mode 3 checks
+ * the integer float->double widening of the mixed form instead. Returns the
  * mismatch count and, if any, one failing pair in example[0..1]. */
 ma_status ma_debug_check_division(int32_t mode, uint64_t n, uint64_t seed, uint64_t* mismatches, double* example);
 

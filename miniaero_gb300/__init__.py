@@ -440,6 +440,9 @@ class Server:
         self._cells[rid.value] = req.nx * req.ny * req.nz
         return rid.value
 
+    def set_max_running_cells(self, cells):
+        check(lib().ma_server_set_max_running_cells(self._h, int(cells)))
+
     def preload(self, req):
         check(lib().ma_server_preload_mesh(self._h, ctypes.byref(req)))
 

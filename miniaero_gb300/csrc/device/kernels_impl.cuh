@@ -52,6 +52,10 @@ __device__ __forceinline__ void store_primitives(const double ut[5], R* __restri
   }
 }
 
+template <class R> __device__ __forceinline__ double to_double(R x);
+template <> __device__ __forceinline__ double to_double<double>(double x) { return x; }
+template <> __device__ __forceinline__ double to_double<float>(float x) { return widen_exact(x); }
+
 template <class R> __device__ __forceinline__ R big_value();
 template <> __device__ __forceinline__ double big_value<double>() { return 1.0e300; }
 template <> __device__ __forceinline__ float big_value<float>() { return FLT_MAX; }
@@ -394,7 +398,7 @@ __device__ __forceinline__ void residual_cell(const TopoView& t, const R* __rest
     const R* fp = fflux + static_cast<size_t>(f) * 5;
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
-      const double v = static_cast<double>(fp[k]);
+      const double v = to_double<R>(fp[k]);
       acc[k] += neg ? -v : v;
     }
   }
@@ -412,7 +416,8 @@ __device__ __forceinline__ void residual_cell(const TopoView& t, const R* __rest
   double ut[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
-    const double r = 0.0 + dtv * acc[k];
+    // 0.0 + x as in apply_cell_flux (it only normalises a -0 result).
+    const double r = std::is_same<R, double>::value ? 0.0 + dtv * acc[k] : dtv * acc[k];
     if (res_out) res_out[k * C + c] = r;
     if (stage == 0) {
       const double un = Un[k * C + c];

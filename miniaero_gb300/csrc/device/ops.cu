@@ -100,6 +100,19 @@ __global__ void k_check_division(int mode, unsigned long long n, unsigned long l
           (static_cast<uint64_t>(__double_as_longlong(m)) & 0x7FF0000000000000ull) - (53ull << 52)));
       a = fma(b, m, b * h);  // a / b close to the midpoint between m and its successor
     }
+    if (mode == 3) {  // widen_exact against the hardware conversion
+      const float f = __uint_as_float(static_cast<uint32_t>(r1));
+      const double w = widen_exact(f);
+      const bool sub = ((static_cast<uint32_t>(r1) >> 23) & 0xFFu) == 0u;
+      const double ref = sub ? __longlong_as_double(static_cast<long long>(static_cast<uint64_t>(r1 & 0x80000000u) << 32))
+                             : static_cast<double>(f);
+      const bool same = (f != f) ? (w != w) : (__double_as_longlong(w) == __double_as_longlong(ref));
+      if (!same && atomicAdd(mismatches, 1ull) == 0ull) {
+        example[0] = static_cast<double>(f);
+        example[1] = w;
+      }
+      continue;
+    }
     const double y = 1.0 / b;
     const double q = div_by_recip(a, b, y);
     const double ref = a / b;

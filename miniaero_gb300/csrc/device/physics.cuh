@@ -42,6 +42,21 @@ __device__ __forceinline__ double div_by_recip(double a, double b, double y) {
 }
 __device__ __forceinline__ float div_by_recip(float a, float /*b*/, float y) { return a * y; }
 
+// float -> double by bit manipulation on the integer pipe (the FP64 pipe is
+// the residual kernel's bottleneck): exact for normal floats, zeros, inf and
+// NaN; FP32 subnormals (|x| < 1.2e-38) become signed zeros.
+__device__ __forceinline__ double widen_exact(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xFFu;
+  const uint32_t sign = u & 0x80000000u;
+  const uint32_t mant = u & 0x7FFFFFu;
+  const uint32_t lo = mant << 29;
+  const uint32_t hi_norm = sign | ((e + 896u) << 20) | (mant >> 3);
+  const uint32_t hi_inf = sign | 0x7FF00000u | (mant >> 3);
+  const uint32_t hi = (e == 0u) ? sign : (e == 0xFFu ? hi_inf : hi_norm);
+  return __hiloint2double(static_cast<int>(hi), e == 0u ? 0 : static_cast<int>(lo));
+}
+
 // Conserved -> primitive (rho, u, v, w, T); always FP64 (the state is FP64).
 __device__ __forceinline__ void primitives(const double U[5], double V[5]) {
   const double gamma = 1.4;

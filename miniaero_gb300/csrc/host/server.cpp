@@ -95,6 +95,8 @@ struct ma_server {
   std::map<MeshKey, CachedMesh> meshes;
   int64_t next_id = 1;
   size_t used = 0;                  // members + cached meshes
+  int64_t max_running_cells = 0;    // 0: no cap
+  int64_t running_cells = 0;
   ma_server_stats stats;
   int64_t busy_start = -1;
 };
@@ -192,6 +194,7 @@ void release_member(ma_server* s, Request& q) {
   q.member = -1;
   s->used -= q.member_bytes;
   q.member_bytes = 0;
+  s->running_cells -= q.cells;
   auto it = s->meshes.find(q.key);
   if (it != s->meshes.end()) it->second.users--;
 }
@@ -205,6 +208,13 @@ void admit(ma_server* s) {
       continue;
     }
     if (s->stats.running >= s->stats.capacity) return;
+    {
+      int64_t C, F;
+      box_counts(q.req, C, F);
+      // Concurrency cap: enough running cells keep the GPU busy; admitting
+      // more only stretches every running request's latency.
+      if (s->max_running_cells > 0 && s->running_cells > 0 && s->running_cells + C > s->max_running_cells) return;
+    }
     const bool cached = s->meshes.count(q.key) != 0;
     const size_t mesh_need = cached ? 0 : dry_mesh_bytes(q.req);
     size_t member_need = dry_member_bytes(s, q.req);
@@ -250,6 +260,7 @@ void admit(ma_server* s) {
     int64_t C, F;
     box_counts(q.req, C, F);
     q.cells = C;
+    s->running_cells += C;
     s->queue.pop_front();
     s->stats.running++;
     s->stats.admitted++;
@@ -389,6 +400,14 @@ extern "C" void ma_server_free(ma_server* s) {
     if (kv.second.host) ma_host_mesh_free(kv.second.host);
   }
   delete s;
+}
+
+extern "C" ma_status ma_server_set_max_running_cells(ma_server* s, int64_t cells) {
+  if (!s || cells < 0) return set_error(MA_EINVAL, "ma_server_set_max_running_cells: bad arguments");
+  std::lock_guard<std::mutex> g(s->mu);
+  s->max_running_cells = cells;
+  s->cv.notify_all();
+  return MA_OK;
 }
 
 extern "C" ma_status ma_server_submit(ma_server* s, const ma_request* r, int64_t* id) {

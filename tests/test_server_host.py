@@ -116,6 +116,23 @@ def test_capacity_limits_running_requests():
     s.close()
 
 
+def test_running_cell_cap_orders_completion():
+    s = server(budget=1 << 40)
+    s.set_max_running_cells(2 * 16 ** 3)
+    ids = [s.submit(req(16, steps=20)) for _ in range(5)]
+    s.poll()
+    assert [s.query(i).state for i in ids] == [s.RUNNING] * 2 + [s.QUEUED] * 3
+    while s.poll():
+        pass
+    fin = [s.query(i).t_finish_ns for i in ids]
+    assert fin[0] <= fin[2] and fin[1] <= fin[3] and fin[3] <= fin[4]
+    big = s.submit(req(32, steps=10))  # larger than the cap: runs alone
+    while s.poll():
+        pass
+    assert s.query(big).state == s.DONE
+    s.close()
+
+
 def test_wait_drives_manual_loop_and_times_out():
     s = server(budget=1 << 40)
     a = s.submit(req(8, steps=40))

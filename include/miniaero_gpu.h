@@ -180,6 +180,19 @@ ma_status ma_solver_check_state(ma_solver* s, int64_t* bad_cell);
 /* One full solve as the reference's Solve(): init + ntimesteps steps. */
 ma_status ma_solver_solve(ma_solver* s, const ma_host_mesh* host_mesh);
 
+/* Allocation-free CFL time step. No counterpart in the reference, which takes
+ * dt from the input file. For callers that cannot allocate device memory at
+ * that point (all memory handed to their own pool, or a loop that must not
+ * block on the allocator): *dt_out = cfl * min_c V_c / sum_f(|u.n| + c|n|),
+ * the value ma_solver_set_state computes, from the device state d_state
+ * (conserved, [5][C] doubles, component-major) on the mesh, with kernels on
+ * `stream` (a cudaStream_t, NULL = legacy default); returns after the stream
+ * has reached the result. Scratch is a fixed 512 KiB array inside the
+ * library; nothing is allocated. Meshes above 16,777,216 cells get MA_EINVAL.
+ * The first call on a device sets up the scratch address (make it before any
+ * stream capture). Calls that overlap on the GPU share the scratch and race. */
+ma_status ma_cfl_dt_noalloc(const ma_mesh* mesh, const double* d_state, double cfl, double* dt_out, void* stream);
+
 /* ---- batched multi-mesh solver ------------------------------------------
  * No reference counterpart as an API: the reference advances one mesh per
  * process (Solve(), TimeSolverExplicitRK4.h:206) and scales out with MPI

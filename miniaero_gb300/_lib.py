@@ -157,6 +157,7 @@ _SIGNATURES = {
     "ma_solver_set_dt": (c_int32, [c_void_p, c_double]),
     "ma_solver_check_state": (c_int32, [c_void_p, ctypes.POINTER(ctypes.c_int64)]),
     "ma_solver_solve": (c_int32, [c_void_p, c_void_p]),
+    "ma_cfl_dt_noalloc": (c_int32, [c_void_p, c_void_p, c_double, P_f64, c_void_p]),
     "ma_batch_create": (c_int32, [ctypes.POINTER(ma_options), c_int32, ctypes.c_size_t, ctypes.POINTER(c_void_p)]),
     "ma_batch_free": (None, [c_void_p]),
     "ma_batch_member_bytes": (ctypes.c_size_t, [c_void_p, c_void_p]),

@@ -34,6 +34,7 @@ DEVICE_SOURCES = [
     ("device/ops.cu", ["--fmad=false"]),
     ("device/solver.cu", ["--fmad=false"]),
     ("device/batch.cu", ["--fmad=false"]),
+    ("device/noalloc.cu", ["--fmad=false"]),
 ]
 HOST_SOURCES = ["host/mesh.cpp", "host/options.cpp", "host/host_api.cpp", "host/server.cpp"]
 

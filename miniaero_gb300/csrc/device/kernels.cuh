@@ -16,9 +16,11 @@ constexpr int kMaxCellFaces = 6;  // Hexa8: every face is internal or boundary
 struct TopoView {
   int32_t C = 0, Fi = 0, Fb = 0, F = 0;
   int32_t nbc_type[4] = {0, 0, 0, 0};  // BC face counts in type order E, T, N, I
-  // Internal faces [0, fi_axis_end[0]) have frames aligned with x, then y up
-  // to fi_axis_end[1], then z up to fi_axis_end[2]; the rest are general.
-  int32_t fi_axis_end[3] = {0, 0, 0};
+  // Internal faces come in classes, class k ending at fi_class_end[k]:
+  // 0..2 frame aligned with axis D = k and both face-to-cell offsets nonzero
+  // only along D; 3..5 frame aligned with axis D = k - 3, general offsets;
+  // then the general faces up to Fi.
+  int32_t fi_class_end[6] = {0, 0, 0, 0, 0, 0};
   const double* vol = nullptr;         // [C]
   const double* vinv = nullptr;        // [C] 1/V rounded to nearest
   const int32_t* fconn = nullptr;      // [2][F] (left, right); right = -1 on a boundary
@@ -27,8 +29,10 @@ struct TopoView {
   const int32_t* csr_grad = nullptr;   // Green-Gauss / min-max / limiter order
   const int32_t* csr_nbr = nullptr;    // neighbour cell of each csr_grad slot (-1 boundary)
   const int32_t* csr_flux = nullptr;   // residual order
-  // 1 where the cell is axis-aligned and its csr_grad list is grouped by axis
+  // Bit 0: the cell is axis-aligned and its csr_grad list is grouped by axis
   // (two faces each for x, y, z): gradient terms along other axes are zero.
+  // Bit 1 (with bit 0): the offset from the cell centre to each face centre
+  // is nonzero only along that face's axis.
   const uint8_t* axis_cell = nullptr;
 };
 

@@ -74,6 +74,119 @@ __device__ __forceinline__ FaceFrame<R> load_frame(const GeomView<R>& g, int f, 
   return fr;
 }
 
+// Running stencil minimum and maximum with the selections the existing
+// kernels make for min_max_face / gather_min_max (StencilLimiter.h:57,246):
+// fmin = (pr < pl) ? pr : pl, fmax = (pr > pl) ? pr : pl, then
+// mn = (fmin < mn) ? fmin : mn, mx = (mx < fmax) ? fmax : mx.
+template <class R>
+struct Extrema {
+  R mn, mx;
+  __device__ __forceinline__ Extrema() : mn(big_value<R>()), mx(-big_value<R>()) {}
+  __device__ __forceinline__ void face(R pl, R pr) {
+    const R fmin_ = (pr < pl) ? pr : pl;
+    const R fmax_ = (pr > pl) ? pr : pl;
+    mn = (fmin_ < mn) ? fmin_ : mn;
+    mx = (mx < fmax_) ? fmax_ : mx;
+  }
+  __device__ __forceinline__ void one(R w) {
+    mn = (w < mn) ? w : mn;
+    mx = (mx < w) ? w : mx;
+  }
+  __device__ __forceinline__ R min() const { return mn; }
+  __device__ __forceinline__ R max() const { return mx; }
+};
+
+// FP64: the same selections made on order keys (integer pipe); the running
+// values are held as injective keys, so the selected double (sign of zero
+// included) comes back exactly. Identical to the compares above for non-NaN
+// values.
+template <>
+struct Extrema<double> {
+  long long mn, mx;
+  __device__ __forceinline__ Extrema() : mn(ikey(big_value<double>())), mx(ikey(-big_value<double>())) {}
+  __device__ __forceinline__ void face(double pl, double pr) {
+    const long long kl = ikey(pl), kr = ikey(pr);
+    const long long cl = ckey(kl), cr = ckey(kr);
+    const bool lt = cr < cl, gt = cr > cl;
+    const long long kmin = lt ? kr : kl, cmin = lt ? cr : cl;
+    const long long kmax = gt ? kr : kl, cmax = gt ? cr : cl;
+    mn = (cmin < ckey(mn)) ? kmin : mn;
+    mx = (ckey(mx) < cmax) ? kmax : mx;
+  }
+  __device__ __forceinline__ void one(double w) {
+    const long long kw = ikey(w), cw = ckey(kw);
+    mn = (cw < ckey(mn)) ? kw : mn;
+    mx = (ckey(mx) < cw) ? kw : mx;
+  }
+  __device__ __forceinline__ double min() const { return from_ikey(mn); }
+  __device__ __forceinline__ double max() const { return from_ikey(mx); }
+};
+
+// Venkatakrishnan limiter of one cell in FP64: min(1, phi_f over its faces)
+// with phi_f = RN(n_f / d_f). Rounding is monotone, so the minimum equals
+// RN(min_f n_f / d_f): the smallest ratio is found with exact
+// cross-multiplied comparisons and divided once per component. AXIS: the
+// cell's offsets are nonzero only along the axis of each face (slots 2p,
+// 2p+1 normal to axis p), so the dot products 0 + dx*gx + dy*gy + dz*gz
+// reduce to their p term (the others are signed zeros for finite gradients,
+// which cannot change a +0-started sum; a zero du is not limited either way).
+template <bool AXIS>
+__device__ __forceinline__ void venkat_cell(const TopoView& t, const GeomView<double>& g, const double wc[5],
+                                            const double mn[5], const double mx[5], const double gsum[5][3],
+                                            double* __restrict__ phi, int c) {
+  const int C = t.C, F = t.F;
+  double nm[5], dm[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) { nm[k] = 1.0; dm[k] = 1.0; }
+  if constexpr (AXIS) {
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+#pragma unroll 1
+      for (int q = 0; q < 2; ++q) {
+        const int code = t.csr_grad[(2 * p + q) * C + c];
+        const int f = code >> 1;
+        const double* dv = (code & 1) ? g.dL : g.dR;
+        const double dp = dv[p * F + f];
+        const double dist = dp * dp;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+          const double du = dp * gsum[k][p];
+          double n, dd;
+          if (venkat_ratio(mx[k] - wc[k], mn[k] - wc[k], du, dist, n, dd) && ratio_less(n, dd, nm[k], dm[k])) {
+            nm[k] = n;
+            dm[k] = dd;
+          }
+        }
+      }
+    }
+  } else {
+#pragma unroll 1
+    for (int s = 0; s < kMaxCellFaces; ++s) {
+      const int code = t.csr_grad[s * C + c];
+      if (code < 0) continue;
+      const int f = code >> 1;
+      const double* dv = (code & 1) ? g.dL : g.dR;
+      const double disp[3] = {dv[f], dv[F + f], dv[2 * F + f]};
+      double dist = 0;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) dist += disp[d] * disp[d];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        double du = 0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) du += disp[d] * gsum[k][d];
+        double n, dd;
+        if (venkat_ratio(mx[k] - wc[k], mn[k] - wc[k], du, dist, n, dd) && ratio_less(n, dd, nm[k], dm[k])) {
+          nm[k] = n;
+          dm[k] = dd;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 5; ++k) phi[k * C + c] = (nm[k] == 1.0 && dm[k] == 1.0) ? 1.0 : nm[k] / dm[k];
+}
+
 // MODE: 0 gradient only (viscous first order), 1 + Venkatakrishnan, 2 + Van Albada.
 template <class R, int MODE>
 __device__ __forceinline__ void sweep1_cell(const TopoView& t, const GeomView<R>& g, const R* __restrict__ W,
@@ -85,15 +198,13 @@ __device__ __forceinline__ void sweep1_cell(const TopoView& t, const GeomView<R>
   const R V = g.vol[c];
   const R Vinv = g.vinv[c];  // RN(1/V), see div_by_recip
   R acc[5][3];
-  R mn[5], mx[5];
+  Extrema<R> ex[5];
 #pragma unroll
-  for (int k = 0; k < 5; ++k) {
+  for (int k = 0; k < 5; ++k)
 #pragma unroll
     for (int d = 0; d < 3; ++d) acc[k][d] = R(0.0);
-    mn[k] = big_value<R>();
-    mx[k] = -big_value<R>();
-  }
-  if (t.axis_cell[c]) {
+  const int ac = t.axis_cell[c];
+  if (ac) {
     // Axis-aligned cell: slots 2p, 2p+1 are its faces normal to axis p, in
     // serial order; only gradient components along p get nonzero terms.
 #pragma unroll
@@ -116,21 +227,13 @@ __device__ __forceinline__ void sweep1_cell(const TopoView& t, const GeomView<R>
             const R pr = left ? wn[k] : wc[k];
             const R gr = R(0.5) * (pl + pr) * np;
             acc[k][p] += left ? div_by_recip(gr, V, Vinv) : div_by_recip(-gr, V, Vinv);
-            if (MODE > 0) {
-              const R fmin_ = (pr < pl) ? pr : pl;
-              const R fmax_ = (pr > pl) ? pr : pl;
-              mn[k] = (fmin_ < mn[k]) ? fmin_ : mn[k];
-              mx[k] = (mx[k] < fmax_) ? fmax_ : mx[k];
-            }
+            if (MODE > 0) ex[k].face(pl, pr);
           }
         } else {
 #pragma unroll
           for (int k = 0; k < 5; ++k) {
             acc[k][p] += div_by_recip(wc[k] * np, V, Vinv);
-            if (MODE > 0) {
-              mn[k] = (wc[k] < mn[k]) ? wc[k] : mn[k];
-              mx[k] = (mx[k] < wc[k]) ? wc[k] : mx[k];
-            }
+            if (MODE > 0) ex[k].one(wc[k]);
           }
         }
       }
@@ -159,22 +262,14 @@ __device__ __forceinline__ void sweep1_cell(const TopoView& t, const GeomView<R>
           const R gr = h * n[d];
           acc[k][d] += left ? div_by_recip(gr, V, Vinv) : div_by_recip(-gr, V, Vinv);
         }
-        if (MODE > 0) {
-          const R fmin_ = (pr < pl) ? pr : pl;
-          const R fmax_ = (pr > pl) ? pr : pl;
-          mn[k] = (fmin_ < mn[k]) ? fmin_ : mn[k];
-          mx[k] = (mx[k] < fmax_) ? fmax_ : mx[k];
-        }
+        if (MODE > 0) ex[k].face(pl, pr);
       }
     } else {
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
 #pragma unroll
         for (int d = 0; d < 3; ++d) acc[k][d] += div_by_recip(wc[k] * n[d], V, Vinv);
-        if (MODE > 0) {
-          mn[k] = (wc[k] < mn[k]) ? wc[k] : mn[k];
-          mx[k] = (mx[k] < wc[k]) ? wc[k] : mx[k];
-        }
+        if (MODE > 0) ex[k].one(wc[k]);
       }
     }
   }
@@ -187,66 +282,45 @@ __device__ __forceinline__ void sweep1_cell(const TopoView& t, const GeomView<R>
       gsum[k][d] = R(0) + acc[k][d];  // green_gauss_gradient_sum
       grad[(3 * k + d) * C + c] = gsum[k][d];
     }
-  if constexpr (MODE == 1 && std::is_same<R, double>::value) {
-    // Venkatakrishnan limiter of the cell: min(1, phi_f over its faces) with
-    // phi_f = RN(n_f / d_f). Rounding is monotone, so the minimum equals
-    // RN(min_f n_f / d_f): the smallest ratio is found with exact
-    // cross-multiplied comparisons and divided once per component.
-    R nm[5], dm[5];
+  if constexpr (MODE > 0) {
+    R mn[5], mx[5];
 #pragma unroll
-    for (int k = 0; k < 5; ++k) { nm[k] = 1.0; dm[k] = 1.0; }
+    for (int k = 0; k < 5; ++k) {
+      mn[k] = ex[k].min();
+      mx[k] = ex[k].max();
+    }
+    if constexpr (MODE == 1 && std::is_same<R, double>::value) {
+      if (ac & 2) venkat_cell<true>(t, g, wc, mn, mx, gsum, phi, c);
+      else venkat_cell<false>(t, g, wc, mn, mx, gsum, phi, c);
+    } else {
+      // Limiter: minimum over this cell's faces of the limiter function.
+      R lim[5];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) lim[k] = R(1.0);
 #pragma unroll 1
-    for (int s = 0; s < kMaxCellFaces; ++s) {
-      const int code = t.csr_grad[s * C + c];
-      if (code < 0) continue;
-      const int f = code >> 1;
-      const R* dv = (code & 1) ? g.dL : g.dR;
-      const R disp[3] = {dv[f], dv[F + f], dv[2 * F + f]};
-      R dist = 0;
+      for (int s = 0; s < kMaxCellFaces; ++s) {
+        const int code = t.csr_grad[s * C + c];
+        if (code < 0) continue;
+        const int f = code >> 1;
+        const R* dv = (code & 1) ? g.dL : g.dR;
+        const R disp[3] = {dv[f], dv[F + f], dv[2 * F + f]};
+        R dist = 0;
 #pragma unroll
-      for (int d = 0; d < 3; ++d) dist += disp[d] * disp[d];
+        for (int d = 0; d < 3; ++d) dist += disp[d] * disp[d];
 #pragma unroll
-      for (int k = 0; k < 5; ++k) {
-        R du = 0;
+        for (int k = 0; k < 5; ++k) {
+          R du = 0;
 #pragma unroll
-        for (int d = 0; d < 3; ++d) du += disp[d] * gsum[k][d];
-        R n, dd;
-        if (venkat_ratio(mx[k] - wc[k], mn[k] - wc[k], du, dist, n, dd) && ratio_less(n, dd, nm[k], dm[k])) {
-          nm[k] = n;
-          dm[k] = dd;
+          for (int d = 0; d < 3; ++d) du += disp[d] * gsum[k][d];
+          const R dumax = mx[k] - wc[k];
+          const R dumin = mn[k] - wc[k];
+          const R p = (MODE == 1) ? venkat<R>(dumax, dumin, du, dist) : vanalbada<R>(dumax, dumin, du);
+          lim[k] = (p < lim[k]) ? p : lim[k];
         }
       }
+#pragma unroll
+      for (int k = 0; k < 5; ++k) phi[k * C + c] = lim[k];
     }
-#pragma unroll
-    for (int k = 0; k < 5; ++k) phi[k * C + c] = (nm[k] == 1.0 && dm[k] == 1.0) ? 1.0 : nm[k] / dm[k];
-  } else if constexpr (MODE > 0) {
-    // Limiter: minimum over this cell's faces of the limiter function.
-    R lim[5];
-#pragma unroll
-    for (int k = 0; k < 5; ++k) lim[k] = R(1.0);
-#pragma unroll 1
-    for (int s = 0; s < kMaxCellFaces; ++s) {
-      const int code = t.csr_grad[s * C + c];
-      if (code < 0) continue;
-      const int f = code >> 1;
-      const R* dv = (code & 1) ? g.dL : g.dR;
-      const R disp[3] = {dv[f], dv[F + f], dv[2 * F + f]};
-      R dist = 0;
-#pragma unroll
-      for (int d = 0; d < 3; ++d) dist += disp[d] * disp[d];
-#pragma unroll
-      for (int k = 0; k < 5; ++k) {
-        R du = 0;
-#pragma unroll
-        for (int d = 0; d < 3; ++d) du += disp[d] * gsum[k][d];
-        const R dumax = mx[k] - wc[k];
-        const R dumin = mn[k] - wc[k];
-        const R p = (MODE == 1) ? venkat<R>(dumax, dumin, du, dist) : vanalbada<R>(dumax, dumin, du);
-        lim[k] = (p < lim[k]) ? p : lim[k];
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < 5; ++k) phi[k * C + c] = lim[k];
   }
 }
 
@@ -286,25 +360,45 @@ __device__ __forceinline__ void internal_flux_face(const TopoView& t, const Geom
     pl[k] = W[k * C + L];
     pr[k] = W[k * C + Rc];
   }
+  int cls = 6;
+#pragma unroll
+  for (int k = 5; k >= 0; --k)
+    if (f < t.fi_class_end[k]) cls = k;
   if (SECOND) {
-    const R dl[3] = {g.dL[f], g.dL[F + f], g.dL[2 * F + f]};
-    const R dr[3] = {g.dR[f], g.dR[F + f], g.dR[2 * F + f]};
+    if (cls < 3) {
+      // Offsets nonzero only along D = cls: the serial dot product
+      // 0 + dx*gx + dy*gy + dz*gz adds signed-zero products that cannot
+      // change an accumulator starting at +0 (finite gradients), so only the
+      // D term is evaluated.
+      const int D = cls;
+      const R dl = g.dL[D * F + f], dr = g.dR[D * F + f];
 #pragma unroll
-    for (int k = 0; k < 5; ++k) {
-      R tl = 0, trr = 0;
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        tl += dl[d] * grad[(3 * k + d) * C + L];
-        trr += dr[d] * grad[(3 * k + d) * C + Rc];
+      for (int k = 0; k < 5; ++k) {
+        const R tl = R(0) + dl * grad[(3 * k + D) * C + L];
+        const R trr = R(0) + dr * grad[(3 * k + D) * C + Rc];
+        pl[k] += tl * phi[k * C + L];
+        pr[k] += trr * phi[k * C + Rc];
       }
-      pl[k] += tl * phi[k * C + L];
-      pr[k] += trr * phi[k * C + Rc];
+    } else {
+      const R dl[3] = {g.dL[f], g.dL[F + f], g.dL[2 * F + f]};
+      const R dr[3] = {g.dR[f], g.dR[F + f], g.dR[2 * F + f]};
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        R tl = 0, trr = 0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          tl += dl[d] * grad[(3 * k + d) * C + L];
+          trr += dr[d] * grad[(3 * k + d) * C + Rc];
+        }
+        pl[k] += tl * phi[k * C + L];
+        pr[k] += trr * phi[k * C + Rc];
+      }
     }
   }
   R flux[5];
-  // Faces [0, axis_end[2]) are axis-aligned, grouped by the axis of their
-  // area vector; the rest take the general path.
-  const int axis = f < t.fi_axis_end[0] ? 0 : f < t.fi_axis_end[1] ? 1 : f < t.fi_axis_end[2] ? 2 : 3;
+  // Classes 0..5 have axis-aligned frames (axis cls % 3); class 6 takes the
+  // general path.
+  const int axis = cls < 6 ? cls % 3 : 3;
   if (axis == 0) face_flux_axis<R, VISC, 0>(t, g, grad, pl, pr, tr, f, L, Rc, flux);
   else if (axis == 1) face_flux_axis<R, VISC, 1>(t, g, grad, pl, pr, tr, f, L, Rc, flux);
   else if (axis == 2) face_flux_axis<R, VISC, 2>(t, g, grad, pl, pr, tr, f, L, Rc, flux);

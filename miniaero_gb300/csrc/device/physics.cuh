@@ -429,14 +429,32 @@ __device__ __forceinline__ R venkat(R dumax, R dumin, R du, R deltax3) {
 // Numerator and denominator of the Venkatakrishnan function, rounded exactly
 // as venkat() rounds them, normalised to n >= 0, d > 0 (both are negated
 // when du < 0, which is exact). Returns false where venkat() returns 1.
+// Order keys: double comparisons on the integer pipe (on GB300 a double
+// compare occupies the FP64 pipe like an add, and that pipe bounds the sweep).
+// ikey(x) is a signed 64-bit key, monotone and injective over all non-NaN
+// doubles, with ikey(-0) = -1 just below ikey(+0) = 0; from_ikey inverts it.
+// ckey moves the negative keys up by one, so -0 and +0 meet: comparing ckeys
+// gives the IEEE result of <, ==, > for every pair of non-NaN doubles.
+__device__ __forceinline__ long long ikey(double x) {
+  const long long b = __double_as_longlong(x);
+  return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFLL);
+}
+__device__ __forceinline__ double from_ikey(long long k) {
+  return __longlong_as_double(k ^ ((k >> 63) & 0x7FFFFFFFFFFFFFFFLL));
+}
+__device__ __forceinline__ long long ckey(long long k) { return k - (k >> 63); }
+__device__ __forceinline__ long long okey(double x) { return ckey(ikey(x)); }
+
 __device__ __forceinline__ bool venkat_ratio(double dumax, double dumin, double du, double eps2, double& n,
                                              double& d) {
-  if (du > 1e-40) {
+  // du > 1e-40 and du < -1e-40 as key comparisons (same result for non-NaN du).
+  const long long kd = okey(du);
+  if (kd > okey(1e-40)) {
     n = (dumax * dumax + eps2) * du + 2 * du * du * dumax;
     d = du * (dumax * dumax + 2 * du * du + dumax * du + eps2);
     return true;
   }
-  if (du < -1e-40) {
+  if (kd < okey(-1e-40)) {
     n = -((dumin * dumin + eps2) * du + 2 * du * du * dumin);
     d = -(du * (dumin * dumin + 2 * du * du + dumin * du + eps2));
     return true;
@@ -446,10 +464,12 @@ __device__ __forceinline__ bool venkat_ratio(double dumax, double dumin, double 
 
 // Exact test n1/d1 < n2/d2 for d1, d2 > 0: compares n1*d2 with n2*d1 as
 // unevaluated sums p + e (p = RN(x*y), e = fma(x, y, -p) exact).
+// The comparisons use order keys (exact for non-NaN values).
 __device__ __forceinline__ bool ratio_less(double n1, double d1, double n2, double d2) {
   const double p1 = n1 * d2, p2 = n2 * d1;
-  if (p1 != p2) return p1 < p2;
-  return fma(n1, d2, -p1) < fma(n2, d1, -p2);
+  const long long k1 = okey(p1), k2 = okey(p2);
+  if (k1 != k2) return k1 < k2;
+  return okey(fma(n1, d2, -p1)) < okey(fma(n2, d1, -p2));
 }
 
 template <class R>

@@ -161,13 +161,23 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
       pass(order, tmp, 0);
       order.swap(tmp);
     }
-    // Axis-aligned faces first, grouped by axis (x, y, z), then the general
-    // ones; (left, right) order within each group. A face is aligned with
-    // axis D when its area vector is nonzero only along D, its tangent only
-    // along (D+2)%3 and its binormal only along (D+1)%3.
-    int32_t axis_end[3] = {0, 0, 0};
+    // Faces grouped by class, (left, right) order within each class. A face
+    // is aligned with axis D when its area vector is nonzero only along D, its
+    // tangent only along (D+2)%3 and its binormal only along (D+1)%3: class D
+    // when in addition both face-to-cell offsets (face centre minus cell
+    // centre, as the geometry below stores them) are nonzero only along D,
+    // class D + 3 otherwise; the general faces are class 6.
+    int32_t class_end[6] = {0, 0, 0, 0, 0, 0};
     {
-      auto face_axis = [&](int32_t i) -> int {
+      auto offsets_along = [&](int32_t i, int D) {
+        const double* x = &v->internal.coords[3 * static_cast<size_t>(i)];
+        const double* xl = &v->cell_coords[3 * static_cast<size_t>(v->internal.conn[2 * i])];
+        const double* xr = &v->cell_coords[3 * static_cast<size_t>(v->internal.conn[2 * i + 1])];
+        for (int d = 0; d < 3; ++d)
+          if (d != D && (x[d] - xl[d] != 0.0 || x[d] - xr[d] != 0.0)) return false;
+        return true;
+      };
+      auto face_class = [&](int32_t i) -> int {
         const double* n = &v->internal.normal[3 * static_cast<size_t>(i)];
         const double* tt = &v->internal.tangent[3 * static_cast<size_t>(i)];
         const double* b = &v->internal.binormal[3 * static_cast<size_t>(i)];
@@ -179,18 +189,18 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
             if (d != T && tt[d] != 0.0) ok = false;
             if (d != B && b[d] != 0.0) ok = false;
           }
-          if (ok) return D;
+          if (ok) return offsets_along(i, D) ? D : D + 3;
         }
-        return 3;
+        return 6;
       };
       std::vector<int32_t> grouped;
       grouped.reserve(Fi);
       std::vector<uint8_t> cls(Fi);
-      for (int32_t i = 0; i < Fi; ++i) cls[i] = static_cast<uint8_t>(face_axis(i));
-      for (int k = 0; k < 4; ++k) {
+      for (int32_t i = 0; i < Fi; ++i) cls[i] = static_cast<uint8_t>(face_class(i));
+      for (int k = 0; k < 7; ++k) {
         for (int32_t g = 0; g < Fi; ++g)
           if (cls[order[g]] == k) grouped.push_back(order[g]);
-        if (k < 3) axis_end[k] = static_cast<int32_t>(grouped.size());
+        if (k < 6) class_end[k] = static_cast<int32_t>(grouped.size());
       }
       order.swap(grouped);
     }
@@ -297,6 +307,16 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
           if (axes[s2] < 0 || ++count[axes[s2]] > 2) ok = false;
         }
         if (!ok) continue;
+        // Bit 1: every face-to-cell offset seen from this cell (x_f - x_c,
+        // geometry rows 13..15 on the left side, 16..18 on the right) is
+        // nonzero only along the face's axis.
+        bool aligned = true;
+        for (size_t s2 = 0; s2 < K; ++s2) {
+          const size_t g = static_cast<size_t>(codes[s2] >> 1);
+          const int base = (codes[s2] & 1) ? 13 : 16;
+          for (int d = 0; d < 3; ++d)
+            if (d != axes[s2] && geo[(base + d) * static_cast<size_t>(F) + g] != 0.0) aligned = false;
+        }
         size_t out = 0;
         for (int d = 0; d < 3; ++d)
           for (size_t s2 = 0; s2 < K; ++s2)
@@ -305,7 +325,7 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
               csr_nbr[out * C + c] = nbrs[s2];
               ++out;
             }
-        axis_cell[c] = 1;
+        axis_cell[c] = aligned ? 3 : 1;
       }
     }
 
@@ -354,7 +374,7 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
     m->topo.Fb = Fb;
     m->topo.F = F;
     for (int r = 0; r < 4; ++r) m->topo.nbc_type[r] = nbc_type[r];
-    for (int k = 0; k < 3; ++k) m->topo.fi_axis_end[k] = axis_end[k];
+    for (int k = 0; k < 6; ++k) m->topo.fi_class_end[k] = class_end[k];
 
     std::vector<float> geo32(geo.size());
     for (size_t i = 0; i < geo.size(); ++i) geo32[i] = static_cast<float>(geo[i]);

@@ -47,6 +47,11 @@ WORKLOADS = {
         problem_type=0, lx=1.0, ly=0.5, lz=0.5, nx=64, ny=64, nz=64, second_order_space=1, viscous=1,
         viscosity_model=1, mu=1.8e-5, prandtl=0.72, ic=1, sod_left=[1.0, 1.0], sod_right=[0.125, 0.1], cfl=0.5,
         ntimesteps=100),
+    # 2,097,152 cells: the mixed form's arrays (~1 GB) exceed L2, for ncu captures of the mixed kernels.
+    "sod_2nd_viscous_128x128x128": dict(
+        problem_type=0, lx=1.0, ly=0.5, lz=0.5, nx=128, ny=128, nz=128, second_order_space=1, viscous=1,
+        viscosity_model=1, mu=1.8e-5, prandtl=0.72, ic=1, sod_left=[1.0, 1.0], sod_right=[0.125, 0.1], cfl=0.5,
+        ntimesteps=100),
     "flat_plate_vanalbada_512x128x128": dict(
         problem_type=1, lx=2.0, ly=0.5, lz=0.5, nx=512, ny=128, nz=128, second_order_space=1, viscous=1,
         limiter=1, viscosity_model=1, mu=1.8e-5, prandtl=0.72, ic=2, cfl=0.5, ntimesteps=50),
@@ -57,17 +62,19 @@ DEFAULT_WORKLOAD = "sod_2nd_viscous_256x128x128"
 def kernel_bytes(md, kind, w):
     """Algorithmic (compulsory) DRAM bytes of one launch: every array the
     kernel touches read or written once, neighbour data counted once (w =
-    bytes of the flux/gradient type). Second-order viscous form, axis-aligned
-    faces (one component each of n, n/|n|, t/|t|, b/|b| plus |n| and the two
-    centroid offsets: 11 values per internal face)."""
+    bytes of the flux/gradient type). Second-order viscous form on axis-aligned
+    faces whose centroid offsets lie along the face axis: the flux reads one
+    component each of n, n/|n|, t/|t|, b/|b|, the two offsets, and |n| (7
+    values per internal face); the sweep one area component and the cell's
+    offset per face."""
     C, Fi = md.ncells, md.internal.nfaces
     Fb = sum(b.nfaces for b in md.bc)
     if kind == "sweep_gradient_limiter":
         # W, V, 1/V, 3 contribution lists, axis flag; writes grad, phi; per face
-        # area vector and centroid offsets.
-        return C * (5 * w + 8 + 8 + 72 + 1 + 15 * w + 5 * w) + Fi * 9 * w + Fb * 6 * w
+        # one area component and the offset of each side.
+        return C * (5 * w + 8 + 8 + 72 + 1 + 15 * w + 5 * w) + Fi * 3 * w + Fb * 2 * w
     if kind == "internal_face_flux":
-        return Fi * (8 + 11 * w + 5 * w) + C * 25 * w
+        return Fi * (8 + 7 * w + 5 * w) + C * 25 * w
     if kind == "boundary_face_flux":
         return Fb * (4 + 16 * w + 5 * w) + Fb * 5 * w
     if kind == "residual_rk_update":
@@ -338,6 +345,7 @@ def run_ours(args, world, rank, local):
     dt = solver.dt
     solver.step(args.warmup)
     solver.synchronize()
+    U_start = solver.get_state()  # state entering the timed region (AOS)
 
     # ---- timed region: K steps from device-resident state ----
     sampler = ClockSampler(local)
@@ -383,9 +391,11 @@ def run_ours(args, world, rank, local):
     eo.cfl = 0.0
     eo.dt = dt
     esolver = ma.TimeSolverExplicitRK4(md, eo, device_mesh=dmesh)
-    hU = torch.empty((C, 5), dtype=torch.float64).pin_memory()
-    hU.numpy()[:] = U0
-    hOut = torch.empty((C, 5), dtype=torch.float64).pin_memory()
+    # Component-major host buffers (MA_LAYOUT_SOA): each step uploads the
+    # state that entered the timed region above and reads back its successor.
+    hU = torch.empty((5, C), dtype=torch.float64).pin_memory()
+    hU.numpy()[:] = U_start.T
+    hOut = torch.empty((5, C), dtype=torch.float64).pin_memory()
     state_bytes = C * 5 * 8
     L = ma._lib.lib()
     inp = ma._lib.f64p(hU.numpy())
@@ -407,6 +417,10 @@ def run_ours(args, world, rank, local):
     e2e_s = allreduce_max(world, time.perf_counter() - t0)
     barrier(world)
     e2e_value = world * C * 4 * args.steps / e2e_s / 1e6
+    # The SoA round trip must give the bits of the same step through the AOS path.
+    esolver.set_state(U_start)
+    esolver.step(1)
+    e2e_verified = bool(np.array_equal(esolver.get_state(), hOut.numpy().T))
     esolver.close()
 
     cpu = None
@@ -435,7 +449,8 @@ def run_ours(args, world, rank, local):
             "clocks": clocks,
             "e2e": {"value": e2e_value, "unit": "Mcell-stage/s", "h2d_bytes_per_step": state_bytes,
                     "d2h_bytes_per_step": state_bytes,
-                    "path": "ma_solver_set_state + ma_solver_step + ma_solver_get_state, pinned host SoA buffers"},
+                    "path": "ma_solver_set_state + ma_solver_step + ma_solver_get_state, pinned host SoA buffers",
+                    "input": "state after the warm-up steps", "verified_vs_aos_path": e2e_verified},
             "gpu_launches": launches,
             "roofline": roofline,
             "kernels": kernels,

@@ -234,16 +234,18 @@ class TimeSolverExplicitRK4:
         self.ncells = mesh_data.ncells
 
     # -- state ---------------------------------------------------------------
-    def set_state(self, U):
-        U = np.ascontiguousarray(U, dtype=np.float64).reshape(self.ncells, 5)
-        check(lib().ma_solver_set_state(self._h, f64p(U), MA_LAYOUT_AOS))
+    def set_state(self, U, layout=MA_LAYOUT_AOS):
+        """U is (ncells, 5) for MA_LAYOUT_AOS, (5, ncells) for MA_LAYOUT_SOA."""
+        shape = (self.ncells, 5) if layout == MA_LAYOUT_AOS else (5, self.ncells)
+        U = np.ascontiguousarray(U, dtype=np.float64).reshape(shape)
+        check(lib().ma_solver_set_state(self._h, f64p(U), int(layout)))
 
     def init_state(self):
         check(lib().ma_solver_init_state(self._h, self.mesh_data._handle))
 
-    def get_state(self):
-        U = np.empty((self.ncells, 5), np.float64)
-        check(lib().ma_solver_get_state(self._h, f64p(U), MA_LAYOUT_AOS))
+    def get_state(self, layout=MA_LAYOUT_AOS):
+        U = np.empty((self.ncells, 5) if layout == MA_LAYOUT_AOS else (5, self.ncells), np.float64)
+        check(lib().ma_solver_get_state(self._h, f64p(U), int(layout)))
         return U
 
     def get_residual(self):

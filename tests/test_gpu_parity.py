@@ -157,6 +157,22 @@ def test_stepping_in_chunks_equals_one_call(has_gpu):
     assert_bitexact(U, run_gpu(md, o, U0))
 
 
+def test_component_major_state_layout(has_gpu):
+    """MA_LAYOUT_SOA ((5, C) host arrays, the layout the end-to-end bench
+    copies) carries the same bits as the cell-major layout."""
+    o = make_options(*REF_TESTS["Ramp_Serial"])
+    o.ntimesteps = 5
+    md = ma.Parallel3DMesh.from_options(o).fill_mesh_data()
+    U0 = ma.initial_state(md, o)
+    with ma.TimeSolverExplicitRK4(md, o) as s:
+        s.set_state(np.ascontiguousarray(U0.T), layout=ma.MA_LAYOUT_SOA)
+        s.step(5)
+        U_soa = s.get_state(layout=ma.MA_LAYOUT_SOA)
+        assert U_soa.shape == (5, md.ncells)
+        assert_bitexact(s.get_state(), U_soa.T)
+    assert_bitexact(U_soa.T, run_gpu(md, o, U0))
+
+
 def test_deterministic_repeat(has_gpu):
     o = make_options(*REF_TESTS["Ramp_Serial"])
     o.ntimesteps = 50

@@ -305,8 +305,9 @@ ma_status ma_debug_binsort(const int32_t* keys, int32_t n, int32_t* perm);
 /* Checks the device's reciprocal-based correctly rounded division against
  * IEEE division on n generated pairs (mode 0 random, 1 divisors with an
  * all-ones significand, 2 quotients near rounding midpoints); mode 3 checks
- * the integer float->double widening of the mixed form instead. Returns the
- * mismatch count and, if any, one failing pair in example[0..1]. */
+ * the integer float->double widening of the mixed form instead, mode 4 its
+ * integer double->float rounding. Returns the mismatch count and, if any,
+ * one failing pair in example[0..1]. */
 ma_status ma_debug_check_division(int32_t mode, uint64_t n, uint64_t seed, uint64_t* mismatches, double* example);
 
 /* ---- operator-level entry points (unit parity; host arrays in and out) --- */

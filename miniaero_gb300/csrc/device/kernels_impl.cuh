@@ -39,11 +39,11 @@ __device__ __forceinline__ void store_primitives(const double ut[5], R* __restri
 #pragma unroll
     for (int k = 0; k < 5; ++k) W[k * C + c] = v[k];
   } else {
-    const float r = static_cast<float>(ut[0]);
+    // narrow_rn: the float conversion, on the integer pipe.
+    const float r = narrow_rn(ut[0]);
     const float ri = 1.0f / r;
-    const float u = static_cast<float>(ut[1]) * ri, v = static_cast<float>(ut[2]) * ri,
-                w = static_cast<float>(ut[3]) * ri;
-    const float e = static_cast<float>(ut[4]) * ri - 0.5f * (u * u + v * v + w * w);
+    const float u = narrow_rn(ut[1]) * ri, v = narrow_rn(ut[2]) * ri, w = narrow_rn(ut[3]) * ri;
+    const float e = narrow_rn(ut[4]) * ri - 0.5f * (u * u + v * v + w * w);
     W[c] = r;
     W[C + c] = u;
     W[2 * C + c] = v;
@@ -187,6 +187,60 @@ __device__ __forceinline__ void venkat_cell(const TopoView& t, const GeomView<do
   for (int k = 0; k < 5; ++k) phi[k * C + c] = (nm[k] == 1.0 && dm[k] == 1.0) ? 1.0 : nm[k] / dm[k];
 }
 
+// Limiter of one cell (MODE 1 Venkatakrishnan in FP32, MODE 2 Van Albada):
+// minimum over its faces of the limiter function, in serial face order.
+// AXIS: offsets along each face's axis only, slots grouped by axis as in
+// venkat_cell; du and |d|^2 reduce to their one nonzero term.
+template <class R, int MODE, bool AXIS>
+__device__ __forceinline__ void limiter_cell(const TopoView& t, const GeomView<R>& g, const R wc[5], const R mn[5],
+                                             const R mx[5], const R gsum[5][3], R* __restrict__ phi, int c) {
+  const int C = t.C, F = t.F;
+  R lim[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) lim[k] = R(1.0);
+  auto apply = [&](int k, R du, R dist) {
+    const R dumax = mx[k] - wc[k];
+    const R dumin = mn[k] - wc[k];
+    const R p = (MODE == 1) ? venkat<R>(dumax, dumin, du, dist) : vanalbada<R>(dumax, dumin, du);
+    lim[k] = (p < lim[k]) ? p : lim[k];
+  };
+  if constexpr (AXIS) {
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const int code = t.csr_grad[(2 * p + q) * C + c];
+        const int f = code >> 1;
+        const R dp = ((code & 1) ? g.dL : g.dR)[p * F + f];
+        const R dist = dp * dp;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) apply(k, dp * gsum[k][p], dist);
+      }
+    }
+  } else {
+#pragma unroll 1
+    for (int s = 0; s < kMaxCellFaces; ++s) {
+      const int code = t.csr_grad[s * C + c];
+      if (code < 0) continue;
+      const int f = code >> 1;
+      const R* dv = (code & 1) ? g.dL : g.dR;
+      const R disp[3] = {dv[f], dv[F + f], dv[2 * F + f]};
+      R dist = 0;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) dist += disp[d] * disp[d];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        R du = 0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) du += disp[d] * gsum[k][d];
+        apply(k, du, dist);
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 5; ++k) phi[k * C + c] = lim[k];
+}
+
 // MODE: 0 gradient only (viscous first order), 1 + Venkatakrishnan, 2 + Van Albada.
 template <class R, int MODE>
 __device__ __forceinline__ void sweep1_cell(const TopoView& t, const GeomView<R>& g, const R* __restrict__ W,
@@ -209,7 +263,7 @@ __device__ __forceinline__ void sweep1_cell(const TopoView& t, const GeomView<R>
     // serial order; only gradient components along p get nonzero terms.
 #pragma unroll
     for (int p = 0; p < 3; ++p) {
-#pragma unroll 1
+#pragma unroll (std::is_same<R, float>::value ? 2 : 1)
       for (int q = 0; q < 2; ++q) {
         const int s = 2 * p + q;
         const int code = t.csr_grad[s * C + c];
@@ -293,33 +347,8 @@ __device__ __forceinline__ void sweep1_cell(const TopoView& t, const GeomView<R>
       if (ac & 2) venkat_cell<true>(t, g, wc, mn, mx, gsum, phi, c);
       else venkat_cell<false>(t, g, wc, mn, mx, gsum, phi, c);
     } else {
-      // Limiter: minimum over this cell's faces of the limiter function.
-      R lim[5];
-#pragma unroll
-      for (int k = 0; k < 5; ++k) lim[k] = R(1.0);
-#pragma unroll 1
-      for (int s = 0; s < kMaxCellFaces; ++s) {
-        const int code = t.csr_grad[s * C + c];
-        if (code < 0) continue;
-        const int f = code >> 1;
-        const R* dv = (code & 1) ? g.dL : g.dR;
-        const R disp[3] = {dv[f], dv[F + f], dv[2 * F + f]};
-        R dist = 0;
-#pragma unroll
-        for (int d = 0; d < 3; ++d) dist += disp[d] * disp[d];
-#pragma unroll
-        for (int k = 0; k < 5; ++k) {
-          R du = 0;
-#pragma unroll
-          for (int d = 0; d < 3; ++d) du += disp[d] * gsum[k][d];
-          const R dumax = mx[k] - wc[k];
-          const R dumin = mn[k] - wc[k];
-          const R p = (MODE == 1) ? venkat<R>(dumax, dumin, du, dist) : vanalbada<R>(dumax, dumin, du);
-          lim[k] = (p < lim[k]) ? p : lim[k];
-        }
-      }
-#pragma unroll
-      for (int k = 0; k < 5; ++k) phi[k * C + c] = lim[k];
+      if (ac & 2) limiter_cell<R, MODE, true>(t, g, wc, mn, mx, gsum, phi, c);
+      else limiter_cell<R, MODE, false>(t, g, wc, mn, mx, gsum, phi, c);
     }
   }
 }
@@ -483,7 +512,7 @@ __device__ __forceinline__ void residual_cell(const TopoView& t, const R* __rest
                                               double* __restrict__ res_out, double dt, int stage, int c) {
   const int C = t.C;
   double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-#pragma unroll 1
+#pragma unroll
   for (int s = 0; s < kMaxCellFaces; ++s) {
     const int code = t.csr_flux[s * C + c];
     if (code < 0) continue;
@@ -491,10 +520,7 @@ __device__ __forceinline__ void residual_cell(const TopoView& t, const R* __rest
     const bool neg = (code & 1) && f < t.Fi;
     const R* fp = fflux + static_cast<size_t>(f) * 5;
 #pragma unroll
-    for (int k = 0; k < 5; ++k) {
-      const double v = to_double<R>(fp[k]);
-      acc[k] += neg ? -v : v;
-    }
+    for (int k = 0; k < 5; ++k) acc[k] += negate_if(to_double<R>(fp[k]), neg);  // sign flip on the integer pipe
   }
   // RK4 coefficients (TimeSolverExplicitRK4.h:188-195): beta of this stage and
   // alpha of the stage that follows (alpha[0] = 0 after the last stage).
@@ -505,8 +531,9 @@ __device__ __forceinline__ void residual_cell(const TopoView& t, const R* __rest
     case 2: beta = 1.0 / 3.0; alpha_next = 1.0; break;
     default: beta = 1.0 / 6.0; alpha_next = 0.0; break;
   }
-  // dt/V as the reference rounds it; the mixed form multiplies by 1/V.
-  const double dtv = std::is_same<R, double>::value ? dt / t.vol[c] : dt * t.vinv[c];
+  // dt/V as the reference rounds it (div_by_recip returns the IEEE quotient);
+  // the mixed form multiplies by 1/V.
+  const double dtv = std::is_same<R, double>::value ? div_by_recip(dt, t.vol[c], t.vinv[c]) : dt * t.vinv[c];
   double ut[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k) {

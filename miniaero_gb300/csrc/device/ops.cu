@@ -100,6 +100,28 @@ __global__ void k_check_division(int mode, unsigned long long n, unsigned long l
           (static_cast<uint64_t>(__double_as_longlong(m)) & 0x7FF0000000000000ull) - (53ull << 52)));
       a = fma(b, m, b * h);  // a / b close to the midpoint between m and its successor
     }
+    if (mode == 4) {  // narrow_rn against the hardware conversion
+      // Random bit patterns (any exponent), values in and next to the float
+      // normal range, exact midpoints between floats and their neighbours.
+      uint64_t bits = r1;
+      const uint32_t kind = static_cast<uint32_t>(r3 & 3u);
+      if (kind >= 1u) {
+        const uint64_t E = 895u + (r2 % 258u);  // 895..1152: both edges of the float range
+        bits = (r1 & 0x800FFFFFFFFFFFFFull) | (E << 52);
+      }
+      if (kind >= 2u) {
+        bits = (bits & ~0x1FFFFFFFull) | 0x10000000ull;  // exact midpoint
+        if (kind == 3u) bits += ((r3 >> 8) & 1u) ? 1u : static_cast<uint64_t>(-1);
+      }
+      const double x = __longlong_as_double(static_cast<long long>(bits));
+      const float got = narrow_rn(x), ref = __double2float_rn(x);
+      const bool same = (ref != ref) ? (got != got) : (__float_as_uint(got) == __float_as_uint(ref));
+      if (!same && atomicAdd(mismatches, 1ull) == 0ull) {
+        example[0] = x;
+        example[1] = static_cast<double>(got);
+      }
+      continue;
+    }
     if (mode == 3) {  // widen_exact against the hardware conversion
       const float f = __uint_as_float(static_cast<uint32_t>(r1));
       const double w = widen_exact(f);

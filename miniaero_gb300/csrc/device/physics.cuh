@@ -14,6 +14,8 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cfloat>
+#include <cstdint>
+#include <type_traits>
 
 namespace miniaero {
 namespace dev {
@@ -57,10 +59,37 @@ __device__ __forceinline__ double widen_exact(float f) {
   return __hiloint2double(static_cast<int>(hi), e == 0u ? 0 : static_cast<int>(lo));
 }
 
+// double -> float rounded to nearest even on the integer pipe (the hardware
+// conversion issues on the FP64 pipe): bit-identical to the conversion for
+// results in the normal float range and for zeros; the other inputs (float
+// subnormals, overflow, inf, NaN) take the hardware conversion.
+__device__ __forceinline__ float narrow_rn(double x) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+  const uint32_t hi = static_cast<uint32_t>(b >> 32), lo = static_cast<uint32_t>(b);
+  const uint32_t E = (hi >> 20) & 0x7FFu;
+  const uint32_t sign = hi & 0x80000000u;
+  if (E >= 897u && E <= 1150u) {
+    uint32_t r = sign | ((E - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    const uint32_t rem = lo & 0x1FFFFFFFu;
+    if (rem > 0x10000000u || (rem == 0x10000000u && (r & 1u))) ++r;  // a carry into the exponent is right
+    return __uint_as_float(r);
+  }
+  if ((hi & 0x7FFFFFFFu) == 0u && lo == 0u) return __uint_as_float(sign);
+  return __double2float_rn(x);
+}
+
+// -x when neg, by flipping the sign bit on the integer pipe (IEEE negation).
+__device__ __forceinline__ double negate_if(double x, bool neg) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (static_cast<long long>(neg) << 63));
+}
+
 // Conserved -> primitive (rho, u, v, w, T); always FP64 (the state is FP64).
+// T = e (gamma - 1) / Rgas is divided through the correctly rounded
+// reciprocal of Rgas (div_by_recip: the IEEE quotient for finite values).
 __device__ __forceinline__ void primitives(const double U[5], double V[5]) {
   const double gamma = 1.4;
   const double Rgas = 287.05;
+  constexpr double kRgasInv = 1.0 / 287.05;
   const double r = U[0];
   const double ri = 1.0 / r;
   const double u = U[1] * ri;
@@ -68,7 +97,7 @@ __device__ __forceinline__ void primitives(const double U[5], double V[5]) {
   const double w = U[3] * ri;
   const double k = 0.5 * (u * u + v * v + w * w);
   const double e = U[4] * ri - k;
-  const double T = e * (gamma - 1.0) / Rgas;
+  const double T = div_by_recip(e * (gamma - 1.0), Rgas, kRgasInv);
   V[0] = r; V[1] = u; V[2] = v; V[3] = w; V[4] = T;
 }
 
@@ -335,19 +364,27 @@ struct Transport {
   double mu;
   double prandtl;
   double k;        // constant model: mu * 1006 / prandtl, rounded as on the device
+  float mu_f, k_f; // mu and k rounded to float on the host (no per-face conversion)
 };
 
 inline Transport make_transport(int model, double mu, double prandtl) {
-  Transport t{model, mu, prandtl, 0.0};
+  Transport t{model, mu, prandtl, 0.0, 0.0f, 0.0f};
   if (model == 1) t.k = mu * 1006.0 / prandtl;
+  t.mu_f = static_cast<float>(t.mu);
+  t.k_f = static_cast<float>(t.k);
   return t;
 }
 
 template <class R>
 __device__ __forceinline__ void transport(const Transport& tr, R T, R& mu, R& k) {
   if (tr.model == 1) {
-    mu = R(tr.mu);
-    k = R(tr.k);
+    if constexpr (std::is_same<R, float>::value) {
+      mu = tr.mu_f;
+      k = tr.k_f;
+    } else {
+      mu = tr.mu;
+      k = tr.k;
+    }
   } else {
     mu = R(1.458e-6) * T * dsqrt<R>(T) / (T + R(110.4));
     k = mu * R(1006.0) / R(0.71);

@@ -9,18 +9,20 @@ namespace miniaero {
 namespace dev {
 
 constexpr int kMaxCellFaces = 6;  // Hexa8: every face is internal or boundary
+constexpr int kFaceTileCells = 4096;  // internal-face order: tiles of this many left cells
 
 // Topology shared by both precisions. Face arrays are in device order:
-// internal faces [0, Fi) sorted by (left, right) cell, then boundary faces
-// [Fi, F) grouped by BC type (Extrapolate, Tangent, NoSlip, Inflow).
+// internal faces [0, Fi) by tile of left cells, class, then (left, right)
+// cell, then boundary faces [Fi, F) grouped by BC type (Extrapolate,
+// Tangent, NoSlip, Inflow).
 struct TopoView {
   int32_t C = 0, Fi = 0, Fb = 0, F = 0;
   int32_t nbc_type[4] = {0, 0, 0, 0};  // BC face counts in type order E, T, N, I
-  // Internal faces come in classes, class k ending at fi_class_end[k]:
-  // 0..2 frame aligned with axis D = k and both face-to-cell offsets nonzero
-  // only along D; 3..5 frame aligned with axis D = k - 3, general offsets;
-  // then the general faces up to Fi.
-  int32_t fi_class_end[6] = {0, 0, 0, 0, 0, 0};
+  // Class of each internal face: 0..2 frame aligned with axis D = class and
+  // both face-to-cell offsets nonzero only along D; 3..5 frame aligned with
+  // axis D = class - 3, general offsets; 6 general. Faces are ordered by
+  // tiles of kFaceTileCells left cells, then class, so warps see one class.
+  const uint8_t* fclass = nullptr;     // [Fi]
   const double* vol = nullptr;         // [C]
   const double* vinv = nullptr;        // [C] 1/V rounded to nearest
   const int32_t* fconn = nullptr;      // [2][F] (left, right); right = -1 on a boundary

@@ -389,10 +389,7 @@ __device__ __forceinline__ void internal_flux_face(const TopoView& t, const Geom
     pl[k] = W[k * C + L];
     pr[k] = W[k * C + Rc];
   }
-  int cls = 6;
-#pragma unroll
-  for (int k = 5; k >= 0; --k)
-    if (f < t.fi_class_end[k]) cls = k;
+  const int cls = t.fclass[f];
   if (SECOND) {
     if (cls < 3) {
       // Offsets nonzero only along D = cls: the serial dot product
@@ -520,7 +517,13 @@ __device__ __forceinline__ void residual_cell(const TopoView& t, const R* __rest
     const bool neg = (code & 1) && f < t.Fi;
     const R* fp = fflux + static_cast<size_t>(f) * 5;
 #pragma unroll
-    for (int k = 0; k < 5; ++k) acc[k] += negate_if(to_double<R>(fp[k]), neg);  // sign flip on the integer pipe
+    for (int k = 0; k < 5; ++k) {
+      const double v = negate_if(to_double<R>(fp[k]), neg);  // sign flip on the integer pipe
+      // The plain form adds to +0 as the reference does (a -0 first term
+      // becomes +0); the mixed form starts from its first term.
+      if (std::is_same<R, float>::value && s == 0) acc[k] = v;
+      else acc[k] += v;
+    }
   }
   // RK4 coefficients (TimeSolverExplicitRK4.h:188-195): beta of this stage and
   // alpha of the stage that follows (alpha[0] = 0 after the last stage).

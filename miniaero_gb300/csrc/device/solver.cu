@@ -161,13 +161,16 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
       pass(order, tmp, 0);
       order.swap(tmp);
     }
-    // Faces grouped by class, (left, right) order within each class. A face
-    // is aligned with axis D when its area vector is nonzero only along D, its
-    // tangent only along (D+2)%3 and its binormal only along (D+1)%3: class D
-    // when in addition both face-to-cell offsets (face centre minus cell
-    // centre, as the geometry below stores them) are nonzero only along D,
-    // class D + 3 otherwise; the general faces are class 6.
-    int32_t class_end[6] = {0, 0, 0, 0, 0, 0};
+    // Face classes. A face is aligned with axis D when its area vector is
+    // nonzero only along D, its tangent only along (D+2)%3 and its binormal
+    // only along (D+1)%3: class D when in addition both face-to-cell offsets
+    // (face centre minus cell centre, as the geometry below stores them) are
+    // nonzero only along D, class D + 3 otherwise; the general faces are
+    // class 6. Device order: tiles of kFaceTileCells left cells, by class
+    // within a tile, (left, right) within a class. A warp then sees one class
+    // (one code path), and the cells a tile's faces read are re-read by the
+    // tile's other classes while they are still in L2.
+    std::vector<uint8_t> fclass_dev(Fi);
     {
       auto offsets_along = [&](int32_t i, int D) {
         const double* x = &v->internal.coords[3 * static_cast<size_t>(i)];
@@ -193,16 +196,19 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
         }
         return 6;
       };
-      std::vector<int32_t> grouped;
-      grouped.reserve(Fi);
       std::vector<uint8_t> cls(Fi);
       for (int32_t i = 0; i < Fi; ++i) cls[i] = static_cast<uint8_t>(face_class(i));
-      for (int k = 0; k < 7; ++k) {
-        for (int32_t g = 0; g < Fi; ++g)
-          if (cls[order[g]] == k) grouped.push_back(order[g]);
-        if (k < 6) class_end[k] = static_cast<int32_t>(grouped.size());
-      }
+      // Stable counting sort of the (left, right) order by (tile, class).
+      const size_t ntiles = static_cast<size_t>(C) / dev::kFaceTileCells + 1;
+      std::vector<int32_t> bucket_start(ntiles * 7 + 1, 0), grouped(Fi);
+      auto bucket = [&](int32_t i) {
+        return static_cast<size_t>(v->internal.conn[2 * i] / dev::kFaceTileCells) * 7 + cls[i];
+      };
+      for (int32_t g = 0; g < Fi; ++g) bucket_start[bucket(order[g]) + 1]++;
+      for (size_t k = 0; k + 1 < bucket_start.size(); ++k) bucket_start[k + 1] += bucket_start[k];
+      for (int32_t g = 0; g < Fi; ++g) grouped[bucket_start[bucket(order[g])]++] = order[g];
       order.swap(grouped);
+      for (int32_t g = 0; g < Fi; ++g) fclass_dev[g] = cls[order[g]];
     }
     std::vector<int32_t> gpu_of_internal(Fi);
     for (int32_t g = 0; g < Fi; ++g) gpu_of_internal[order[g]] = g;
@@ -338,6 +344,7 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
       m.topo.csr_nbr = a.take<int32_t>(K * C);
       m.topo.csr_flux = a.take<int32_t>(K * C);
       m.topo.axis_cell = a.take<uint8_t>(C);
+      m.topo.fclass = a.take<uint8_t>(static_cast<size_t>(Fi));
       double* g64 = a.take<double>(19 * static_cast<size_t>(F));
       float* g32 = a.take<float>(19 * static_cast<size_t>(F));
       double* vol64 = const_cast<double*>(m.topo.vol);
@@ -374,7 +381,6 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
     m->topo.Fb = Fb;
     m->topo.F = F;
     for (int r = 0; r < 4; ++r) m->topo.nbc_type[r] = nbc_type[r];
-    for (int k = 0; k < 6; ++k) m->topo.fi_class_end[k] = class_end[k];
 
     std::vector<float> geo32(geo.size());
     for (size_t i = 0; i < geo.size(); ++i) geo32[i] = static_cast<float>(geo[i]);
@@ -395,6 +401,7 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
     if (e == cudaSuccess) e = copy(m->topo.csr_nbr, csr_nbr.data(), sizeof(int32_t) * csr_nbr.size());
     if (e == cudaSuccess) e = copy(m->topo.csr_flux, csr_flux.data(), sizeof(int32_t) * csr_flux.size());
     if (e == cudaSuccess) e = copy(m->topo.axis_cell, axis_cell.data(), axis_cell.size());
+    if (e == cudaSuccess && Fi > 0) e = copy(m->topo.fclass, fclass_dev.data(), fclass_dev.size());
     if (e == cudaSuccess) e = copy(m->g64.fn, geo.data(), sizeof(double) * geo.size());
     if (e == cudaSuccess) e = copy(m->g32.fn, geo32.data(), sizeof(float) * geo32.size());
     if (e == cudaSuccess) e = copy(m->g32.vol, vol32.data(), sizeof(float) * vol32.size());

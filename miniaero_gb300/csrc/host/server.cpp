@@ -116,7 +116,7 @@ size_t dry_member_bytes(const ma_server* s, const ma_request& r) {
 size_t dry_mesh_bytes(const ma_request& r) {
   int64_t C, F;
   box_counts(r, C, F);
-  return static_cast<size_t>(C) * 100 + static_cast<size_t>(F) * 236 + 16 * 256;
+  return static_cast<size_t>(C) * 100 + static_cast<size_t>(F) * 237 + 16 * 256;
 }
 
 MeshKey key_of(const ma_request& r) {

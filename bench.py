@@ -198,12 +198,12 @@ def load_peaks():
         return 6800.0, "fallback"
 
 
-def load_traffic(kernel):
-    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if any."""
+def load_traffic(key):
+    """One table of the committed ncu summary (profiles/ncu_traffic.json), if any."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     try:
         with open(path) as f:
-            return json.load(f).get(kernel)
+            return json.load(f).get(key)
     except Exception:
         return None
 
@@ -383,7 +383,14 @@ def run_ours(args, world, rank, local):
     Um = msolver.get_state()
     errs = [float(np.linalg.norm(Um[:, k] - U_fp64[:, k]) / max(np.linalg.norm(U_fp64[:, k]), 1e-300))
             for k in range(5)]
+    # Momentum components whose FP64 values are near zero (transverse momentum
+    # in Sod) give large ratios above; these scale by the momentum magnitude.
+    mom = max(float(np.linalg.norm(U_fp64[:, 1:4])), 1e-300)
+    errs_mom = [float(np.linalg.norm(Um[:, k] - U_fp64[:, k]) / mom) for k in (1, 2, 3)]
     mprof = msolver.profile_steps(2)
+    # FP32 work arrays: algorithmic bytes at 4 bytes per value, against HBM.
+    mroofline, mkernels = kernel_rooflines(md, mprof, 4, clocks.get("sm_mhz"))
+    mroofline["traffic"] = (load_traffic("traffic_bytes_per_launch_mixed") or {}).get(mroofline["kernel"])
     msolver.close()
 
     # ---- end to end through the C ABI with pinned host buffers ----
@@ -456,8 +463,9 @@ def run_ours(args, world, rank, local):
             "kernels": kernels,
             "mixed": {"value": mvalue, "unit": "Mcell-stage/s", "ms_per_step": mms / args.steps,
                       "speedup_vs_fp64": mvalue / value, "rel_l2_error_vs_fp64": errs,
+                      "momentum_error_vs_fp64_momentum_norm": errs_mom,
                       "error_after_steps": int(steps_fp64),
-                      "kernels": {k: {"ms_per_launch": v[0] / v[1], "launches": v[1]} for k, v in mprof.items()}},
+                      "roofline": mroofline, "kernels": mkernels},
             "cpu_baseline": cpu,
             "batched": batched,
             "serving": serving,

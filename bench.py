@@ -582,6 +582,7 @@ def run_serving(ma, n_requests=32, rate=200.0, nsteps=500, seed=1, budget=150 <<
     done = sum(1 for i in infos if i.state == 2)
     cell_stages = sum(i.cells * 4 * nsteps for i in infos if i.state == 2)
     offered = sum(n ** 3 * 4 * nsteps for _, n, _ in reqs) / (reqs[-1][0] if reqs[-1][0] > 0 else 1.0)
+    static = run_static_batch(ma, phys, reqs, budget)
     return {"workload": "Poisson %.0f/s flat-plate requests, Mach U[0.1,0.6], sizes {32..128}^3, %d steps, mixed"
                         % (rate, nsteps),
             "requests": n_requests, "completed": done, "tick_steps": tick, "budget_bytes": budget,
@@ -595,7 +596,46 @@ def run_serving(ma, n_requests=32, rate=200.0, nsteps=500, seed=1, budget=150 <<
             "queue_wait_s": {"p50": float(np.percentile(queue, 50)), "p99": float(np.percentile(queue, 99))},
             "peak_running": st["peak_running"], "peak_bytes": st["peak_bytes"],
             "offered_load_mcell_stage_s": offered / 1e6,
-            "saturated": bool(offered / 1e6 > cell_stages / wall / 1e6)}
+            "saturated": bool(offered / 1e6 > cell_stages / wall / 1e6),
+            "batched_same_requests": static,
+            "serving_vs_batched": (cell_stages / wall / 1e6) / static["value"]}
+
+
+def run_static_batch(ma, phys, reqs, budget, steps=40, warmup=3):
+    """The serving stream's requests as one static batch (all resident from
+    the start, stepped together, autotuned): the batched form's throughput
+    on the serving workload."""
+    import torch
+    meshes = {}
+    b = ma.Batch(phys, capacity=len(reqs), budget_bytes=budget)
+    cells = 0
+    for _, n, mach in reqs:
+        o = phys.copy()
+        o.nx = o.ny = o.nz = n
+        o.lx, o.ly, o.lz = 2.0, 0.5, 0.5
+        o.inflow_state = flat_plate_inflow(mach)
+        o.inflow_given = 1
+        if n not in meshes:
+            md = ma.Parallel3DMesh.from_options(o).fill_mesh_data()
+            meshes[n] = (md, ma.DeviceMesh(md))
+        md, dm = meshes[n]
+        b.add(dm, ma.initial_state(md, o), inflow_state=flat_plate_inflow(mach))
+        cells += md.ncells
+    b.autotune(reps=2)
+    b.step(warmup)
+    b.synchronize()
+    stream = torch.cuda.ExternalStream(b.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.step(steps)
+    e1.record(stream)
+    b.synchronize()
+    ms = e0.elapsed_time(e1)
+    b.close()
+    for md, dm in meshes.values():
+        dm.close()
+    return {"value": cells * 4 * steps / (ms / 1e3) / 1e6, "unit": "Mcell-stage/s", "members": len(reqs),
+            "cells": cells, "timed_steps": steps}
 
 
 def main():

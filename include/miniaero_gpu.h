@@ -121,6 +121,39 @@ void ma_options_default(ma_options* o);
  * MA_EINVAL), not a silent default. */
 ma_status ma_options_read(const char* path, ma_options* o);
 
+/* ---- run controls and checkpoints ---------------------------------------
+ * No counterpart in the reference, whose only output is results.<rank>
+ * (TimeSolverExplicitRK4.h:514-538). Run controls are extra lines of the same
+ * input file, one per line ("checkpoint <path>", "checkpoint_frequency <n>",
+ * "restart <path>"); ma_options_read skips them. */
+#define MA_PATH_MAX 512
+typedef struct {
+  char checkpoint_path[MA_PATH_MAX];  /* "" = no checkpoints */
+  int32_t checkpoint_frequency;       /* steps between checkpoints; 0 = only at the end */
+  char restart_path[MA_PATH_MAX];     /* "" = start from the initial conditions */
+} ma_run_options;
+void ma_run_options_default(ma_run_options* r);
+ma_status ma_run_options_read(const char* path, ma_run_options* r);
+
+typedef struct {
+  int64_t ncells;
+  int64_t steps_done;   /* RK4 steps behind the state */
+  double time;          /* simulated time of the state */
+  double dt;            /* the run's time step (restarts keep it) */
+  uint64_t mesh_hash;   /* ma_mesh_hash of the mesh the state belongs to */
+} ma_checkpoint_info;
+/* 64-bit hash of a mesh's cell count, cell centroids and volumes, and face
+ * set sizes and types: a restart checks it against the checkpoint's. */
+uint64_t ma_mesh_hash(const ma_mesh_view* view);
+/* Writes the conserved state U (ncells x 5 in `layout`) with its header and
+ * a payload checksum; the file appears under `path` only once complete. */
+ma_status ma_checkpoint_write(const char* path, const ma_checkpoint_info* info, const double* U, int32_t layout);
+/* Reads the header into *info and, when U is not NULL, the state (at most
+ * max_cells cells) in `layout`. MA_EIO: unreadable, truncated or checksum
+ * mismatch; MA_EINVAL: not a checkpoint, other version, too many cells. */
+ma_status ma_checkpoint_read(const char* path, ma_checkpoint_info* info, double* U, int64_t max_cells,
+                             int32_t layout);
+
 /* ---- host mesh (replaces Parallel3DMesh + MeshProcessor, single rank) ---- */
 /* Parallel3DMesh::Parallel3DMesh + fillMeshData (kokkos/Parallel3DMesh.C:36,
  * Parallel3DMesh.h:173-449): builds cells, faces, BC sets and the face

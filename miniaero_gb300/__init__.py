@@ -16,6 +16,7 @@ All numerical work runs on the GPU through the library; a missing library or
 GPU raises MiniaeroError instead of falling back to the CPU.
 """
 import ctypes
+import os
 
 import numpy as np
 
@@ -27,7 +28,8 @@ from ._lib import (MA_BC_EXTRAPOLATE, MA_BC_INFLOW, MA_BC_NOSLIP, MA_BC_TANGENT,
 
 __all__ = [
     "Options", "Parallel3DMesh", "MeshData", "FaceSet", "DeviceMesh", "TimeSolverExplicitRK4",
-    "initial_state", "roe_flux", "viscous_flux", "venkat_limit", "vanalbada_limit", "compute_primitives",
+    "initial_state", "mesh_hash", "checkpoint_write", "checkpoint_read", "run_options_read",
+    "roe_flux", "viscous_flux", "venkat_limit", "vanalbada_limit", "compute_primitives",
     "device_count", "MiniaeroError", "BC_NAMES",
     "MA_BC_EXTRAPOLATE", "MA_BC_TANGENT", "MA_BC_INFLOW", "MA_BC_NOSLIP",
     "MA_LIMITER_VENKAT", "MA_LIMITER_VANALBADA", "MA_VISC_SUTHERLAND", "MA_VISC_CONSTANT",
@@ -196,6 +198,38 @@ def initial_state(mesh_data, options):
     return U
 
 
+def mesh_hash(mesh_data):
+    """ma_mesh_hash: 64-bit hash of the mesh a checkpoint belongs to."""
+    v = mesh_data.view()
+    return int(lib().ma_mesh_hash(ctypes.byref(v)))
+
+
+def checkpoint_write(path, U, steps_done, time, dt, mesh_hash_value):
+    """Writes the conserved state U (ncells, 5) as a checkpoint file."""
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    info = _lib.ma_checkpoint_info(U.shape[0], int(steps_done), float(time), float(dt), int(mesh_hash_value))
+    check(lib().ma_checkpoint_write(os.fsencode(path), ctypes.byref(info), f64p(U), MA_LAYOUT_AOS))
+
+
+def checkpoint_read(path):
+    """Reads a checkpoint: (info dict, U of shape (ncells, 5))."""
+    info = _lib.ma_checkpoint_info()
+    check(lib().ma_checkpoint_read(os.fsencode(path), ctypes.byref(info), ctypes.cast(None, _lib.P_f64), 0,
+                                   MA_LAYOUT_AOS))
+    U = np.empty((info.ncells, 5), np.float64)
+    check(lib().ma_checkpoint_read(os.fsencode(path), ctypes.byref(info), f64p(U), info.ncells, MA_LAYOUT_AOS))
+    return {"ncells": info.ncells, "steps_done": info.steps_done, "time": info.time, "dt": info.dt,
+            "mesh_hash": info.mesh_hash}, U
+
+
+def run_options_read(path):
+    """ma_run_options_read: the checkpoint / restart lines of an input file."""
+    r = _lib.ma_run_options()
+    check(lib().ma_run_options_read(os.fsencode(path), ctypes.byref(r)))
+    return {"checkpoint_path": r.checkpoint_path.decode(), "checkpoint_frequency": r.checkpoint_frequency,
+            "restart_path": r.restart_path.decode()}
+
+
 class DeviceMesh:
     """Device copy of a MeshData (ma_mesh_upload); shareable by solvers."""
 
@@ -266,6 +300,22 @@ class TimeSolverExplicitRK4:
         self.step(self.options.ntimesteps)
         self.synchronize()
         return self.get_state()
+
+    def save_checkpoint(self, path):
+        """Writes the current state, step count and dt to a checkpoint file."""
+        self.synchronize()
+        n = self.steps_done
+        checkpoint_write(path, self.get_state(), n, n * self.dt, self.dt, mesh_hash(self.mesh_data))
+
+    def restore_checkpoint(self, path):
+        """Continues from a checkpoint of this mesh: state and dt; returns the
+        checkpoint's step count (steps_done restarts from 0)."""
+        info, U = checkpoint_read(path)
+        if info["ncells"] != self.ncells or info["mesh_hash"] != mesh_hash(self.mesh_data):
+            raise MiniaeroError(_lib.MA_EINVAL, "%s was written for a different mesh" % path)
+        self.set_state(U)
+        self.dt = info["dt"]
+        return info["steps_done"]
 
     def profile_steps(self, nsteps):
         """Steps with CUDA events around each kernel; {kind: (ms_total, launches)}."""

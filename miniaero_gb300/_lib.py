@@ -80,6 +80,24 @@ class ma_mesh_view(ctypes.Structure):
     ]
 
 
+MA_PATH_MAX = 512
+
+
+class ma_run_options(ctypes.Structure):
+    _fields_ = [
+        ("checkpoint_path", ctypes.c_char * MA_PATH_MAX),
+        ("checkpoint_frequency", c_int32),
+        ("restart_path", ctypes.c_char * MA_PATH_MAX),
+    ]
+
+
+class ma_checkpoint_info(ctypes.Structure):
+    _fields_ = [
+        ("ncells", ctypes.c_int64), ("steps_done", ctypes.c_int64),
+        ("time", c_double), ("dt", c_double), ("mesh_hash", ctypes.c_uint64),
+    ]
+
+
 class ma_request(ctypes.Structure):
     _fields_ = [
         ("nx", c_int32), ("ny", c_int32), ("nz", c_int32), ("problem_type", c_int32),
@@ -134,6 +152,12 @@ _SIGNATURES = {
     "ma_device_count": (c_int32, []),
     "ma_options_default": (None, [ctypes.POINTER(ma_options)]),
     "ma_options_read": (c_int32, [ctypes.c_char_p, ctypes.POINTER(ma_options)]),
+    "ma_run_options_default": (None, [ctypes.POINTER(ma_run_options)]),
+    "ma_run_options_read": (c_int32, [ctypes.c_char_p, ctypes.POINTER(ma_run_options)]),
+    "ma_mesh_hash": (ctypes.c_uint64, [ctypes.POINTER(ma_mesh_view)]),
+    "ma_checkpoint_write": (c_int32, [ctypes.c_char_p, ctypes.POINTER(ma_checkpoint_info), P_f64, c_int32]),
+    "ma_checkpoint_read": (c_int32, [ctypes.c_char_p, ctypes.POINTER(ma_checkpoint_info), P_f64, ctypes.c_int64,
+                                     c_int32]),
     "ma_host_mesh_build": (c_int32, [ctypes.POINTER(ma_options), ctypes.POINTER(c_void_p)]),
     "ma_host_mesh_view": (c_int32, [c_void_p, ctypes.POINTER(ma_mesh_view)]),
     "ma_host_mesh_free": (None, [c_void_p]),

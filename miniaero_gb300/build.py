@@ -36,7 +36,7 @@ DEVICE_SOURCES = [
     ("device/batch.cu", ["--fmad=false"]),
     ("device/noalloc.cu", ["--fmad=false"]),
 ]
-HOST_SOURCES = ["host/mesh.cpp", "host/options.cpp", "host/host_api.cpp", "host/server.cpp"]
+HOST_SOURCES = ["host/mesh.cpp", "host/options.cpp", "host/host_api.cpp", "host/server.cpp", "host/checkpoint.cpp"]
 
 
 def _nvcc():

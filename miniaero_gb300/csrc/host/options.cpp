@@ -112,6 +112,10 @@ extern "C" ma_status ma_options_read(const char* path, ma_options* o) {
       if (si < 0 || bi < 0) ok = false; else o->bc_override[si] = bi;
     } else if (key == "keep_residual") {
       in >> o->keep_residual;
+    } else if (key == "checkpoint" || key == "restart") {
+      std::string v; in >> v;  // run controls, read by ma_run_options_read
+    } else if (key == "checkpoint_frequency") {
+      int32_t v; in >> v;
     } else {
       return set_error(MA_EINVAL, std::string(path) + ": unknown option '" + key + "'");
     }

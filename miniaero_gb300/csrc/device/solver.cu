@@ -14,12 +14,14 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <new>
 #include <string>
 #include <vector>
 
 #include "../../../include/miniaero_gpu.h"
 #include "../host/errors.hpp"
+#include "../host/parallel.hpp"
 #include "batch_internal.hpp"
 #include "kernels.cuh"
 
@@ -146,21 +148,7 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
     const int32_t Fb = static_cast<int32_t>(Fb64);
     const int32_t F = Fi + Fb;
 
-    // Device order of internal faces: by (left, right), two stable counting sorts.
-    std::vector<int32_t> order(Fi), tmp(Fi), cnt(static_cast<size_t>(C) + 1);
-    {
-      const int32_t* conn = v->internal.conn;
-      auto pass = [&](const std::vector<int32_t>& in, std::vector<int32_t>& outv, int side) {
-        std::fill(cnt.begin(), cnt.end(), 0);
-        for (int32_t i : in) cnt[conn[2 * i + side] + 1]++;
-        for (int32_t c = 0; c < C; ++c) cnt[c + 1] += cnt[c];
-        for (int32_t i : in) outv[cnt[conn[2 * i + side]]++] = i;
-      };
-      for (int32_t i = 0; i < Fi; ++i) tmp[i] = i;
-      pass(tmp, order, 1);
-      pass(order, tmp, 0);
-      order.swap(tmp);
-    }
+    std::vector<int32_t> order(Fi);  // device position -> internal face index
     // Face classes. A face is aligned with axis D when its area vector is
     // nonzero only along D, its tangent only along (D+2)%3 and its binormal
     // only along (D+1)%3: class D when in addition both face-to-cell offsets
@@ -197,17 +185,48 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
         return 6;
       };
       std::vector<uint8_t> cls(Fi);
-      for (int32_t i = 0; i < Fi; ++i) cls[i] = static_cast<uint8_t>(face_class(i));
-      // Stable counting sort of the (left, right) order by (tile, class).
-      const size_t ntiles = static_cast<size_t>(C) / dev::kFaceTileCells + 1;
-      std::vector<int32_t> bucket_start(ntiles * 7 + 1, 0), grouped(Fi);
-      auto bucket = [&](int32_t i) {
-        return static_cast<size_t>(v->internal.conn[2 * i] / dev::kFaceTileCells) * 7 + cls[i];
-      };
-      for (int32_t g = 0; g < Fi; ++g) bucket_start[bucket(order[g]) + 1]++;
-      for (size_t k = 0; k + 1 < bucket_start.size(); ++k) bucket_start[k + 1] += bucket_start[k];
-      for (int32_t g = 0; g < Fi; ++g) grouped[bucket_start[bucket(order[g])]++] = order[g];
-      order.swap(grouped);
+      miniaero::parallel_for(static_cast<size_t>(Fi), [&](size_t b, size_t e) {
+        for (size_t i = b; i < e; ++i) cls[i] = static_cast<uint8_t>(face_class(static_cast<int32_t>(i)));
+      });
+      // Sort by (tile of left, class, left, right, index): a stable LSD radix
+      // sort (11-bit digits) of (key, index) words with key = tile | class |
+      // left within the tile, then the right cell orders each run of equal
+      // keys (a cell is the left cell of at most 6 faces).
+      static_assert((dev::kFaceTileCells & (dev::kFaceTileCells - 1)) == 0, "tile size is a power of two");
+      constexpr int kTileShift = __builtin_ctz(dev::kFaceTileCells);
+      int tile_bits = 0;
+      while ((static_cast<uint64_t>(C - 1) >> (kTileShift + tile_bits)) != 0) ++tile_bits;
+      const int key_bits = tile_bits + 3 + kTileShift;  // < 33 for C < 2^30
+      const int32_t* conn = v->internal.conn;
+      std::vector<uint64_t> words(Fi), tmp(Fi);
+      miniaero::parallel_for(static_cast<size_t>(Fi), [&](size_t b, size_t e) {
+        for (size_t i = b; i < e; ++i) {
+          const uint64_t L = static_cast<uint32_t>(conn[2 * i]);
+          const uint64_t key = ((L >> kTileShift) << (3 + kTileShift)) | (static_cast<uint64_t>(cls[i]) << kTileShift) |
+                               (L & (dev::kFaceTileCells - 1));
+          words[i] = (key << 30) | i;  // Fi < 2^30
+        }
+      });
+      for (int shift = 30; shift < 30 + key_bits; shift += 11) {
+        size_t count[2048] = {0};
+        for (const uint64_t w : words) count[(w >> shift) & 2047]++;
+        size_t acc = 0;
+        for (size_t& c : count) { const size_t n = c; c = acc; acc += n; }
+        for (const uint64_t w : words) tmp[count[(w >> shift) & 2047]++] = w;
+        words.swap(tmp);
+      }
+      for (int32_t g = 0; g < Fi; ++g) order[g] = static_cast<int32_t>(words[g] & ((1ull << 30) - 1));
+      for (int32_t g = 0; g < Fi;) {  // runs of one left cell and class: order by right cell
+        int32_t e = g + 1;
+        while (e < Fi && (words[e] >> 30) == (words[g] >> 30)) ++e;
+        for (int32_t a = g + 1; a < e; ++a) {
+          const int32_t x = order[a];
+          int32_t b = a - 1;
+          while (b >= g && conn[2 * order[b] + 1] > conn[2 * x + 1]) { order[b + 1] = order[b]; --b; }
+          order[b + 1] = x;
+        }
+        g = e;
+      }
       for (int32_t g = 0; g < Fi; ++g) fclass_dev[g] = cls[order[g]];
     }
     std::vector<int32_t> gpu_of_internal(Fi);
@@ -229,7 +248,11 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
 
     // Host staging of face data in device order.
     std::vector<int32_t> fconn(2 * static_cast<size_t>(F));
-    std::vector<double> geo(19 * static_cast<size_t>(F), 0.0);  // fn3 fnu3 ftu3 fbu3 fnn1 dL3 dR3
+    // fn3 fnu3 ftu3 fbu3 fnn1 dL3 dR3; every entry is written below (no zero fill
+    // of the ~150 B per face up front: the writes spread over the threads).
+    const size_t geo_size = 19 * static_cast<size_t>(F);
+    std::unique_ptr<double[]> geo_buf(new double[geo_size]);
+    double* const geo = geo_buf.get();
     auto put_face = [&](int32_t g, const ma_face_set& s, int32_t i, bool internal) {
       const int32_t L = s.conn[2 * i];
       const int32_t R = internal ? s.conn[2 * i + 1] : -1;
@@ -249,11 +272,15 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
         geo[(6 + d) * static_cast<size_t>(F) + g] = t[d] / tn;
         geo[(9 + d) * static_cast<size_t>(F) + g] = b[d] / bn;
         geo[(13 + d) * static_cast<size_t>(F) + g] = x[d] - v->cell_coords[3 * static_cast<size_t>(L) + d];
-        if (internal) geo[(16 + d) * static_cast<size_t>(F) + g] = x[d] - v->cell_coords[3 * static_cast<size_t>(R) + d];
+        geo[(16 + d) * static_cast<size_t>(F) + g] =
+            internal ? x[d] - v->cell_coords[3 * static_cast<size_t>(R) + d] : 0.0;
       }
       geo[12 * static_cast<size_t>(F) + g] = nn;
     };
-    for (int32_t i = 0; i < Fi; ++i) put_face(gpu_of_internal[i], v->internal, i, true);
+    // In device order (sequential writes, gathered reads), on the host's threads.
+    miniaero::parallel_for(static_cast<size_t>(Fi), [&](size_t b, size_t e) {
+      for (size_t g = b; g < e; ++g) put_face(static_cast<int32_t>(g), v->internal, order[g], true);
+    });
     for (int b = 0; b < v->nbc; ++b)
       for (int32_t i = 0; i < v->bc[b].nfaces; ++i) put_face(bc_base[b] + i, v->bc[b], i, false);
 
@@ -382,8 +409,10 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
     m->topo.F = F;
     for (int r = 0; r < 4; ++r) m->topo.nbc_type[r] = nbc_type[r];
 
-    std::vector<float> geo32(geo.size());
-    for (size_t i = 0; i < geo.size(); ++i) geo32[i] = static_cast<float>(geo[i]);
+    std::unique_ptr<float[]> geo32(new float[geo_size]);
+    miniaero::parallel_for(geo_size, [&](size_t b, size_t e) {
+      for (size_t i = b; i < e; ++i) geo32[i] = static_cast<float>(geo[i]);
+    });
     std::vector<float> vol32(C), vinv32(C);
     std::vector<double> vinv64(C);
     for (int32_t c = 0; c < C; ++c) {
@@ -402,8 +431,8 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
     if (e == cudaSuccess) e = copy(m->topo.csr_flux, csr_flux.data(), sizeof(int32_t) * csr_flux.size());
     if (e == cudaSuccess) e = copy(m->topo.axis_cell, axis_cell.data(), axis_cell.size());
     if (e == cudaSuccess && Fi > 0) e = copy(m->topo.fclass, fclass_dev.data(), fclass_dev.size());
-    if (e == cudaSuccess) e = copy(m->g64.fn, geo.data(), sizeof(double) * geo.size());
-    if (e == cudaSuccess) e = copy(m->g32.fn, geo32.data(), sizeof(float) * geo32.size());
+    if (e == cudaSuccess) e = copy(m->g64.fn, geo, sizeof(double) * geo_size);
+    if (e == cudaSuccess) e = copy(m->g32.fn, geo32.get(), sizeof(float) * geo_size);
     if (e == cudaSuccess) e = copy(m->g32.vol, vol32.data(), sizeof(float) * vol32.size());
     if (e == cudaSuccess) e = copy(m->g64.vinv, vinv64.data(), sizeof(double) * vinv64.size());
     if (e == cudaSuccess) e = copy(m->g32.vinv, vinv32.data(), sizeof(float) * vinv32.size());

@@ -4,8 +4,12 @@
 #include "mesh.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <vector>
+
+#include "parallel.hpp"
 
 namespace miniaero {
 
@@ -57,24 +61,35 @@ std::vector<int32_t> binsort_permutation(const int32_t* keys, int32_t n, int32_t
   auto bin_of = [&](int32_t i) -> int32_t {
     return static_cast<int32_t>(mul * (keys[static_cast<size_t>(i) * stride] - kmin));
   };
-  std::vector<int32_t> count(static_cast<size_t>(nbins), 0), offset(static_cast<size_t>(nbins), 0);
-  for (int32_t i = 0; i < n; ++i) count[bin_of(i)]++;
-  int32_t acc = 0;
-  for (int32_t b = 0; b < nbins; ++b) { offset[b] = acc; acc += count[b]; }
-  std::vector<int32_t> fill(static_cast<size_t>(nbins), 0);
-  for (int32_t i = 0; i < n; ++i) {
-    const int32_t b = bin_of(i);
-    order[offset[b] + fill[b]++] = i;
+  // Stable binning in index order = a stable sort of (bin, index) pairs by
+  // bin, done as an LSD radix sort (11-bit digits): sequential passes instead
+  // of per-bin counters hit in shuffled order.
+  std::vector<uint64_t> pairs(static_cast<size_t>(n)), tmp(static_cast<size_t>(n));
+  for (int32_t i = 0; i < n; ++i)
+    pairs[i] = (static_cast<uint64_t>(bin_of(i)) << 32) | static_cast<uint32_t>(i);
+  for (int shift = 32; (static_cast<uint64_t>(nbins - 1) >> (shift - 32)) > 0; shift += 11) {
+    size_t count[2048] = {0};
+    for (const uint64_t p : pairs) count[(p >> shift) & 2047]++;
+    size_t acc = 0;
+    for (size_t& c : count) { const size_t v = c; c = acc; acc += v; }
+    for (const uint64_t p : pairs) tmp[count[(p >> shift) & 2047]++] = p;
+    pairs.swap(tmp);
   }
+  for (int32_t k = 0; k < n; ++k) order[k] = static_cast<int32_t>(pairs[k] & 0xFFFFFFFFu);
   auto key = [&](int32_t i) { return keys[static_cast<size_t>(i) * stride]; };
-  for (int32_t b = 0; b < nbins; ++b) {
-    if (count[b] <= 1) continue;
+  // Bubble pass within each bin (each run of equal bins).
+  for (int32_t first = 0; first < n;) {
+    int32_t last = first + 1;
+    while (last < n && (pairs[last] >> 32) == (pairs[first] >> 32)) ++last;
+    const int32_t begin = first, count_b = last - first;
+    first = last;
+    if (count_b <= 1) continue;
     bool sorted = false;
-    int32_t upper = offset[b] + count[b];
+    int32_t upper = begin + count_b;
     while (!sorted) {
       sorted = true;
-      int32_t old_idx = order[offset[b]];
-      for (int32_t k = offset[b] + 1; k < upper; ++k) {
+      int32_t old_idx = order[begin];
+      for (int32_t k = begin + 1; k < upper; ++k) {
         const int32_t new_idx = order[k];
         if (!(key(old_idx) < key(new_idx))) {
           order[k - 1] = new_idx;
@@ -220,15 +235,19 @@ void fill_face_set(HostFaceSet& fs, const std::vector<RawFace>& raw, const std::
   fs.normal.resize(n * 3);
   fs.tangent.resize(n * 3);
   fs.binormal.resize(n * 3);
-  for (size_t i = 0; i < n; ++i) {
-    const RawFace& f = raw[static_cast<size_t>(ids[i])];
-    fs.conn[2 * i] = f.cv_minus;
-    fs.conn[2 * i + 1] = f.cv_plus;
-    fs.flux_index[2 * i] = f.flux_minus;
-    fs.flux_index[2 * i + 1] = f.flux_plus;
-    face_geometry(f.nodes, xyz, &fs.coords[3 * i], &fs.normal[3 * i], &fs.tangent[3 * i],
-                  &fs.binormal[3 * i]);
-  }
+  // Faces come in shuffled order, so the node lookups are random: spread
+  // them over the host's threads.
+  parallel_for(n, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; ++i) {
+      const RawFace& f = raw[static_cast<size_t>(ids[i])];
+      fs.conn[2 * i] = f.cv_minus;
+      fs.conn[2 * i + 1] = f.cv_plus;
+      fs.flux_index[2 * i] = f.flux_minus;
+      fs.flux_index[2 * i + 1] = f.flux_plus;
+      face_geometry(f.nodes, xyz, &fs.coords[3 * i], &fs.normal[3 * i], &fs.tangent[3 * i],
+                    &fs.binormal[3 * i]);
+    }
+  });
   fs.permutation = binsort_permutation(fs.conn.data(), fs.nfaces, 2);
 }
 
@@ -317,22 +336,27 @@ std::string build_box_mesh(const MeshSpec& spec, HostMesh& out) {
   out.ncells = ncells;
   out.cell_coords.resize(static_cast<size_t>(ncells) * 3);
   out.cell_volumes.resize(static_cast<size_t>(ncells));
-  int negative = 0;
-  for (int32_t ie = 0; ie < ncells; ++ie) {
-    const int32_t* en = &conn[static_cast<size_t>(ie) * 8];
-    double ex[8], ey[8], ez[8];
-    double sx = 0, sy = 0, sz = 0;
-    for (int j = 0; j < 8; ++j) {
-      ex[j] = xyz[static_cast<size_t>(en[j]) * 3];
-      ey[j] = xyz[static_cast<size_t>(en[j]) * 3 + 1];
-      ez[j] = xyz[static_cast<size_t>(en[j]) * 3 + 2];
+  std::atomic<int> negative_total{0};
+  parallel_for(static_cast<size_t>(ncells), [&](size_t b, size_t e) {
+    int negative = 0;
+    for (size_t ie = b; ie < e; ++ie) {
+      const int32_t* en = &conn[ie * 8];
+      double ex[8], ey[8], ez[8];
+      double sx = 0, sy = 0, sz = 0;
+      for (int j = 0; j < 8; ++j) {
+        ex[j] = xyz[static_cast<size_t>(en[j]) * 3];
+        ey[j] = xyz[static_cast<size_t>(en[j]) * 3 + 1];
+        ez[j] = xyz[static_cast<size_t>(en[j]) * 3 + 2];
+      }
+      out.cell_volumes[ie] = hexa8_volume(ex, ey, ez, &negative);
+      for (int j = 0; j < 8; ++j) { sx += ex[j]; sy += ey[j]; sz += ez[j]; }
+      out.cell_coords[3 * ie] = sx / 8;
+      out.cell_coords[3 * ie + 1] = sy / 8;
+      out.cell_coords[3 * ie + 2] = sz / 8;
     }
-    out.cell_volumes[ie] = hexa8_volume(ex, ey, ez, &negative);
-    for (int j = 0; j < 8; ++j) { sx += ex[j]; sy += ey[j]; sz += ez[j]; }
-    out.cell_coords[3 * static_cast<size_t>(ie)] = sx / 8;
-    out.cell_coords[3 * static_cast<size_t>(ie) + 1] = sy / 8;
-    out.cell_coords[3 * static_cast<size_t>(ie) + 2] = sz / 8;
-  }
+    negative_total += negative;
+  });
+  const int negative = negative_total.load();
   if (negative) {
     std::fprintf(stderr, "miniaero: warning: %d Gauss points with Jacobian determinant < 1e-300\n", negative);
   }

@@ -40,6 +40,7 @@ enum { MA_BC_EXTRAPOLATE = 0, MA_BC_TANGENT = 1, MA_BC_INFLOW = 2, MA_BC_NOSLIP 
 enum { MA_LIMITER_VENKAT = 0, MA_LIMITER_VANALBADA = 1 };
 enum { MA_VISC_SUTHERLAND = 0, MA_VISC_CONSTANT = 1 };
 enum { MA_PREC_FP64 = 0, MA_PREC_MIXED = 1 };
+enum { MA_GATHER_ATOMICS = 0, MA_GATHER_CELL_FLUX = 1 };
 /* State layouts: AOS is View<double*[5]> LayoutRight (U[c*5+k], the
  * reference's host layout); SOA is U[k*ncells+c]. */
 enum { MA_LAYOUT_AOS = 0, MA_LAYOUT_SOA = 1 };
@@ -73,6 +74,10 @@ typedef struct {
   double inflow_state[5];     /* conserved inflow / constant state */
   int32_t bc_override[6];     /* per side (bottom, top, front, back, right, left), -1 = default map */
   int32_t keep_residual;      /* 1: keep the last stage residual on the device */
+  int32_t gather;             /* MA_GATHER_*: the reference's default -DATOMICS_FLUX
+                                 reduction order, or its -DCELL_FLUX build (per-slot
+                                 storage summed in slot order; needs a mesh uploaded
+                                 with MA_MESH_CELL_FLUX) */
 } ma_options;
 
 /* One face list; mirrors Faces<Device> (kokkos/Faces.h:42-71). Vector
@@ -170,6 +175,13 @@ ma_status ma_host_initial_state(const ma_host_mesh* m, const ma_options* o, doub
  * per-face Roe frame and the per-cell ordered contribution lists that replay
  * the reference's serial accumulation order. */
 ma_status ma_mesh_upload(const ma_mesh_view* view, ma_mesh** out);
+/* As ma_mesh_upload; flags MA_MESH_CELL_FLUX also builds the per-cell lists
+ * in element-local slot order (from every face set's flux_index) that
+ * solvers and batches with gather = MA_GATHER_CELL_FLUX use (72 more bytes
+ * per cell). No reference counterpart as a call: it stands for the
+ * reference's compile-time choice of -DCELL_FLUX. */
+#define MA_MESH_CELL_FLUX 1
+ma_status ma_mesh_upload_ex(const ma_mesh_view* view, int32_t flags, ma_mesh** out);
 void ma_mesh_free(ma_mesh* m);
 /* Device bytes held by the mesh. */
 size_t ma_mesh_device_bytes(const ma_mesh* m);
@@ -339,8 +351,9 @@ ma_status ma_debug_binsort(const int32_t* keys, int32_t n, int32_t* perm);
  * IEEE division on n generated pairs (mode 0 random, 1 divisors with an
  * all-ones significand, 2 quotients near rounding midpoints); mode 3 checks
  * the integer float->double widening of the mixed form instead, mode 4 its
- * integer double->float rounding. Returns the mismatch count and, if any,
- * one failing pair in example[0..1]. */
+ * integer double->float rounding; mode 5 divides tiny, subnormal and zero
+ * numerators. Returns the mismatch count and, if any, one failing pair in
+ * example[0..1]. */
 ma_status ma_debug_check_division(int32_t mode, uint64_t n, uint64_t seed, uint64_t* mismatches, double* example);
 
 /* ---- operator-level entry points (unit parity; host arrays in and out) --- */

@@ -113,13 +113,16 @@ class FaceSet:
         self.tangent = arr(fs.tangent, (n, 3), np.float64)
         self.binormal = arr(fs.binormal, (n, 3), np.float64)
         self.permutation = arr(fs.permutation, (n,), np.int32)
+        # Element-local face slots of (left, right) (Faces.h:109-110), when given.
+        self.flux_index = arr(fs.flux_index, (n, 2), np.int32) if (n == 0 or fs.flux_index) else None
 
     def to_c(self):
         fs = _lib.ma_face_set()
         fs.nfaces = self.nfaces
         fs.type = self.type
         fs.conn = i32p(self.conn)
-        fs.flux_index = ctypes.cast(None, _lib.P_i32)
+        fi = getattr(self, "flux_index", None)
+        fs.flux_index = i32p(fi) if fi is not None else ctypes.cast(None, _lib.P_i32)
         fs.coords = f64p(self.coords)
         fs.normal = f64p(self.normal)
         fs.tangent = f64p(self.tangent)
@@ -233,11 +236,13 @@ def run_options_read(path):
 class DeviceMesh:
     """Device copy of a MeshData (ma_mesh_upload); shareable by solvers."""
 
-    def __init__(self, mesh_data):
+    def __init__(self, mesh_data, cell_flux=False):
+        """cell_flux: also build the slot-order lists of gather = MA_GATHER_CELL_FLUX."""
         self._mesh_data = mesh_data
         self._view = mesh_data.view()
         self._h = ctypes.c_void_p()
-        check(lib().ma_mesh_upload(ctypes.byref(self._view), ctypes.byref(self._h)))
+        flags = _lib.MA_MESH_CELL_FLUX if cell_flux else 0
+        check(lib().ma_mesh_upload_ex(ctypes.byref(self._view), flags, ctypes.byref(self._h)))
         self.ncells = mesh_data.ncells
 
     @property
@@ -262,7 +267,8 @@ class TimeSolverExplicitRK4:
     def __init__(self, mesh_data, options, device_mesh=None):
         self.options = options.copy()
         self.mesh_data = mesh_data
-        self.device_mesh = device_mesh if device_mesh is not None else DeviceMesh(mesh_data)
+        self.device_mesh = device_mesh if device_mesh is not None else DeviceMesh(
+            mesh_data, cell_flux=self.options.gather == _lib.MA_GATHER_CELL_FLUX)
         self._h = ctypes.c_void_p()
         check(lib().ma_solver_create(self.device_mesh._h, ctypes.byref(self.options.c), ctypes.byref(self._h)))
         self.ncells = mesh_data.ncells

@@ -14,6 +14,8 @@ MA_BC_EXTRAPOLATE, MA_BC_TANGENT, MA_BC_INFLOW, MA_BC_NOSLIP = range(4)
 MA_LIMITER_VENKAT, MA_LIMITER_VANALBADA = 0, 1
 MA_VISC_SUTHERLAND, MA_VISC_CONSTANT = 0, 1
 MA_PREC_FP64, MA_PREC_MIXED = 0, 1
+MA_GATHER_ATOMICS, MA_GATHER_CELL_FLUX = 0, 1
+MA_MESH_CELL_FLUX = 1
 MA_LAYOUT_AOS, MA_LAYOUT_SOA = 0, 1
 MA_IC_REFERENCE, MA_IC_SOD, MA_IC_CONSTANT = 0, 1, 2
 MA_MAX_BC_SETS = 16
@@ -52,6 +54,7 @@ class ma_options(ctypes.Structure):
         ("inflow_state", c_double * 5),
         ("bc_override", c_int32 * 6),
         ("keep_residual", c_int32),
+        ("gather", c_int32),
     ]
 
 
@@ -163,6 +166,7 @@ _SIGNATURES = {
     "ma_host_mesh_free": (None, [c_void_p]),
     "ma_host_initial_state": (c_int32, [c_void_p, ctypes.POINTER(ma_options), P_f64]),
     "ma_mesh_upload": (c_int32, [ctypes.POINTER(ma_mesh_view), ctypes.POINTER(c_void_p)]),
+    "ma_mesh_upload_ex": (c_int32, [ctypes.POINTER(ma_mesh_view), c_int32, ctypes.POINTER(c_void_p)]),
     "ma_mesh_free": (None, [c_void_p]),
     "ma_mesh_device_bytes": (ctypes.c_size_t, [c_void_p]),
     "ma_solver_create": (c_int32, [c_void_p, ctypes.POINTER(ma_options), ctypes.POINTER(c_void_p)]),

@@ -41,7 +41,8 @@ int main(int argc, char** argv) {
   ma_mesh_view view;
   ma_host_mesh_view(hm, &view);
   ma_mesh* dm = nullptr;
-  if ((st = ma_mesh_upload(&view, &dm)) != MA_OK) return fail("mesh upload", st);
+  const int32_t upload_flags = o.gather == MA_GATHER_CELL_FLUX ? MA_MESH_CELL_FLUX : 0;
+  if ((st = ma_mesh_upload_ex(&view, upload_flags, &dm)) != MA_OK) return fail("mesh upload", st);
   std::fprintf(stdout, "\n ... Setup time: %8.2f seconds ...\n", seconds_since(t_setup));
 
   ma_solver* s = nullptr;

@@ -37,6 +37,7 @@ namespace {
 struct Member {
   int32_t id = -1;
   ma_mesh* mesh = nullptr;
+  int gather = MA_GATHER_ATOMICS;  // list order of the batch's options
   void* dmem = nullptr;
   size_t bytes = 0;
   double dt = 0.0;
@@ -100,7 +101,7 @@ size_t member_bytes(const ma_batch* b, const ma_mesh* m) {
 template <class R>
 dev::Segment<R> make_segment(const Member& m, const dev::StageBuffers<R>& sb) {
   dev::Segment<R> s;
-  s.t = miniaero::mesh_topo(m.mesh);
+  s.t = miniaero::mesh_topo(m.mesh, m.gather);
   s.g = miniaero::mesh_geom<R>(m.mesh);
   s.b = sb;
   s.s = m.st;
@@ -195,6 +196,7 @@ extern "C" ma_status ma_batch_create(const ma_options* o, int32_t capacity, size
   if (!o || !out || capacity <= 0) return set_error(MA_EINVAL, "ma_batch_create: bad arguments");
   *out = nullptr;
   if (o->precision != MA_PREC_FP64 && o->precision != MA_PREC_MIXED) return set_error(MA_EINVAL, "bad precision");
+  if (o->gather != MA_GATHER_ATOMICS && o->gather != MA_GATHER_CELL_FLUX) return set_error(MA_EINVAL, "bad gather");
   std::unique_ptr<ma_batch> b(new (std::nothrow) ma_batch);
   if (!b) return set_error(MA_ENOMEM, "ma_batch_create: out of host memory");
   b->opts = *o;
@@ -203,6 +205,7 @@ extern "C" ma_status ma_batch_create(const ma_options* o, int32_t capacity, size
   b->cfg.viscous = o->viscous != 0;
   b->cfg.limiter = o->limiter;
   b->cfg.transport = dev::make_transport(o->viscosity_model, o->mu, o->prandtl);
+  b->cfg.cell_flux = o->gather == MA_GATHER_CELL_FLUX;
   b->capacity = capacity;
   b->budget = budget_bytes;
   MB_CUDA_TRY(cudaGetDevice(&b->device));
@@ -243,8 +246,11 @@ extern "C" ma_status ma_batch_add(ma_batch* b, ma_mesh* mesh, const double* U0, 
   const size_t need = member_bytes(b, mesh);
   if (b->used + need > b->budget) return set_error(MA_EBUDGET, "member does not fit the device-memory budget");
   if (!(dt > 0.0) && !(b->opts.cfl > 0.0)) return set_error(MA_EINVAL, "ma_batch_add: dt must be > 0 without cfl");
+  if (b->opts.gather == MA_GATHER_CELL_FLUX && !miniaero::mesh_has_cell_flux(mesh))
+    return set_error(MA_EINVAL, "gather cell_flux needs a mesh uploaded with MA_MESH_CELL_FLUX");
   Member m;
   m.mesh = mesh;
+  m.gather = b->opts.gather;
   m.bytes = need;
   for (int k = 0; k < 5; ++k) m.inflow[k] = inflow_state ? inflow_state[k] : b->opts.inflow_state[k];
   cudaError_t e = cudaMalloc(&m.dmem, need);

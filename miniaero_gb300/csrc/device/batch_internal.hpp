@@ -9,6 +9,10 @@ namespace miniaero {
 size_t mesh_cells(const ma_mesh* m);
 size_t mesh_faces(const ma_mesh* m);
 dev::TopoView mesh_topo(const ma_mesh* m);
+// The mesh's lists in the given MA_GATHER_* order (the CELL_FLUX lists exist
+// when the mesh was uploaded with MA_MESH_CELL_FLUX).
+dev::TopoView mesh_topo(const ma_mesh* m, int gather);
+bool mesh_has_cell_flux(const ma_mesh* m);
 template <class R>
 dev::GeomView<R> mesh_geom(const ma_mesh* m);
 template <>

@@ -87,6 +87,7 @@ struct Segment {
 struct PathConfig {
   bool second_order = false;
   bool viscous = false;
+  bool cell_flux = false;  // -DCELL_FLUX residual reduction (lists in slot order)
   int limiter = 0;  // 0 Venkatakrishnan, 1 Van Albada
   Transport transport{0, 0.0, 0.0, 0.0};
   double inflow[5] = {0, 0, 0, 0, 0};

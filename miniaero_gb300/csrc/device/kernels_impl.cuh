@@ -246,26 +246,16 @@ __device__ __forceinline__ void limiter_cell(const TopoView& t, const GeomView<R
   for (int k = 0; k < 5; ++k) phi[k * C + c] = lim[k];
 }
 
-// MODE: 0 gradient only (viscous first order), 1 + Venkatakrishnan, 2 + Van Albada.
-template <class R, int MODE>
-__device__ __forceinline__ void sweep1_cell(const TopoView& t, const GeomView<R>& g, const R* __restrict__ W,
-                                            R* __restrict__ grad, R* __restrict__ phi, int c) {
+// Green-Gauss terms of one cell added into acc in the reference's serial
+// face order (GreenGauss.h:79-220), div(a) giving each term a / V; with
+// MINMAX the stencil min/max too. Axis-aligned cells (axis_cell bit 0): slots
+// 2p, 2p+1 are the faces normal to axis p, in serial order, and only the
+// gradient components along p get nonzero terms.
+template <class R, bool MINMAX, class Div>
+__device__ __forceinline__ void green_gauss_cell(const TopoView& t, const GeomView<R>& g, const R* __restrict__ W,
+                                                 int c, const R wc[5], R acc[5][3], Extrema<R>* ex, Div div) {
   const int C = t.C, F = t.F;
-  R wc[5];
-#pragma unroll
-  for (int k = 0; k < 5; ++k) wc[k] = W[k * C + c];
-  const R V = g.vol[c];
-  const R Vinv = g.vinv[c];  // RN(1/V), see div_by_recip
-  R acc[5][3];
-  Extrema<R> ex[5];
-#pragma unroll
-  for (int k = 0; k < 5; ++k)
-#pragma unroll
-    for (int d = 0; d < 3; ++d) acc[k][d] = R(0.0);
-  const int ac = t.axis_cell[c];
-  if (ac) {
-    // Axis-aligned cell: slots 2p, 2p+1 are its faces normal to axis p, in
-    // serial order; only gradient components along p get nonzero terms.
+  if (t.axis_cell[c]) {
 #pragma unroll
     for (int p = 0; p < 3; ++p) {
 #pragma unroll (std::is_same<R, float>::value ? 2 : 1)
@@ -285,20 +275,20 @@ __device__ __forceinline__ void sweep1_cell(const TopoView& t, const GeomView<R>
             const R pl = left ? wc[k] : wn[k];
             const R pr = left ? wn[k] : wc[k];
             const R gr = R(0.5) * (pl + pr) * np;
-            acc[k][p] += left ? div_by_recip(gr, V, Vinv) : div_by_recip(-gr, V, Vinv);
-            if (MODE > 0) ex[k].face(pl, pr);
+            acc[k][p] += div(left ? gr : -gr);
+            if (MINMAX) ex[k].face(pl, pr);
           }
         } else {
 #pragma unroll
           for (int k = 0; k < 5; ++k) {
-            acc[k][p] += div_by_recip(wc[k] * np, V, Vinv);
-            if (MODE > 0) ex[k].one(wc[k]);
+            acc[k][p] += div(wc[k] * np);
+            if (MINMAX) ex[k].one(wc[k]);
           }
         }
       }
     }
-  } else {
-  // Gradient contributions and min/max, in the reference's serial face order.
+    return;
+  }
 #pragma unroll 1
   for (int s = 0; s < kMaxCellFaces; ++s) {
     const int code = t.csr_grad[s * C + c];
@@ -319,28 +309,81 @@ __device__ __forceinline__ void sweep1_cell(const TopoView& t, const GeomView<R>
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
           const R gr = h * n[d];
-          acc[k][d] += left ? div_by_recip(gr, V, Vinv) : div_by_recip(-gr, V, Vinv);
+          acc[k][d] += div(left ? gr : -gr);
         }
-        if (MODE > 0) ex[k].face(pl, pr);
+        if (MINMAX) ex[k].face(pl, pr);
       }
     } else {
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
 #pragma unroll
-        for (int d = 0; d < 3; ++d) acc[k][d] += div_by_recip(wc[k] * n[d], V, Vinv);
-        if (MODE > 0) ex[k].one(wc[k]);
+        for (int d = 0; d < 3; ++d) acc[k][d] += div(wc[k] * n[d]);
+        if (MINMAX) ex[k].one(wc[k]);
       }
     }
   }
+}
+
+// The gradient of one cell with every term divided by IEEE division, written
+// as 0 + sum: the rare path for cells whose reciprocal-method terms may be
+// inexact (quotients near the underflow threshold). Out of line, so its
+// registers do not weigh on the sweep.
+__device__ __noinline__ void gradient_exact(const TopoView& t, const GeomView<double>& g, const double* __restrict__ W,
+                                            double* __restrict__ grad, int c) {
+  const int C = t.C;
+  double wc[5], acc[5][3];
+  for (int k = 0; k < 5; ++k) {
+    wc[k] = W[k * C + c];
+    for (int d = 0; d < 3; ++d) acc[k][d] = 0.0;
   }
-  R gsum[5][3];
+  const double V = g.vol[c];
+  green_gauss_cell<double, false>(t, g, W, c, wc, acc, static_cast<Extrema<double>*>(nullptr),
+                                  [&](double a) { return a / V; });
+  for (int k = 0; k < 5; ++k)
+    for (int d = 0; d < 3; ++d) grad[(3 * k + d) * C + c] = 0.0 + acc[k][d];
+}
+
+// MODE: 0 gradient only (viscous first order), 1 + Venkatakrishnan, 2 + Van Albada.
+template <class R, int MODE>
+__device__ __forceinline__ void sweep1_cell(const TopoView& t, const GeomView<R>& g, const R* __restrict__ W,
+                                            R* __restrict__ grad, R* __restrict__ phi, int c) {
+  const int C = t.C;
+  R wc[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) wc[k] = W[k * C + c];
+  const R V = g.vol[c];
+  const R Vinv = g.vinv[c];  // RN(1/V), see div_by_recip
+  R acc[5][3];
+  Extrema<R> ex[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k)
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      gsum[k][d] = R(0) + acc[k][d];  // green_gauss_gradient_sum
-      grad[(3 * k + d) * C + c] = gsum[k][d];
+    for (int d = 0; d < 3; ++d) acc[k][d] = R(0.0);
+  const int ac = t.axis_cell[c];
+  bool inexact = false;  // some term's reciprocal quotient may differ from the IEEE one
+  green_gauss_cell<R, (MODE > 0)>(t, g, W, c, wc, acc, ex,
+                                  [&](R a) { return div_by_recip_flag(a, V, Vinv, inexact); });
+  R gsum[5][3];
+  bool exact_done = false;
+  if constexpr (std::is_same<R, double>::value) {
+    if (inexact) {  // rare: tiny quotients; redo the cell's sums with IEEE division
+      gradient_exact(t, g, W, grad, c);
+#pragma unroll
+      for (int k = 0; k < 5; ++k)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) gsum[k][d] = grad[(3 * k + d) * C + c];
+      exact_done = true;
     }
+  }
+  if (!exact_done) {
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        gsum[k][d] = R(0) + acc[k][d];  // green_gauss_gradient_sum
+        grad[(3 * k + d) * C + c] = gsum[k][d];
+      }
+  }
   if constexpr (MODE > 0) {
     R mn[5], mx[5];
 #pragma unroll
@@ -508,11 +551,18 @@ __device__ __forceinline__ void bc_flux_face(const TopoView& t, const GeomView<R
 }
 
 // Ordered residual gather + RK4 update + primitives of the next stage state.
+// cell_flux: the reference's -DCELL_FLUX reduction, r = 0 + sum over the
+// slots (in slot order) of dt/V * flux (Flux.h:214-224), instead of
+// r = 0 + dt/V * (0 + sum of the fluxes in the atomic order).
 template <class R>
 __device__ __forceinline__ void residual_cell(const TopoView& t, const R* __restrict__ fflux, double* __restrict__ Un,
                                               double* __restrict__ Unp1, R* __restrict__ W,
-                                              double* __restrict__ res_out, double dt, int stage, int c) {
+                                              double* __restrict__ res_out, double dt, int stage, bool cell_flux,
+                                              int c) {
   const int C = t.C;
+  // dt/V as the reference rounds it (div_by_recip returns the IEEE quotient);
+  // the mixed form multiplies by 1/V.
+  const double dtv = std::is_same<R, double>::value ? div_by_recip(dt, t.vol[c], t.vinv[c]) : dt * t.vinv[c];
   double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
 #pragma unroll
   for (int s = 0; s < kMaxCellFaces; ++s) {
@@ -524,10 +574,13 @@ __device__ __forceinline__ void residual_cell(const TopoView& t, const R* __rest
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
       const double v = negate_if(to_double<R>(fp[k]), neg);  // sign flip on the integer pipe
-      // The plain form adds to +0 as the reference does (a -0 first term
-      // becomes +0); the mixed form starts from its first term.
-      if (std::is_same<R, float>::value && s == 0) acc[k] = v;
-      else acc[k] += v;
+      if (cell_flux) {
+        acc[k] = acc[k] + dtv * v;
+      } else if (std::is_same<R, float>::value && s == 0) {
+        acc[k] = v;  // the mixed form starts from its first term
+      } else {
+        acc[k] += v;  // the plain form adds to +0 as the reference does
+      }
     }
   }
   // RK4 coefficients (TimeSolverExplicitRK4.h:188-195): beta of this stage and
@@ -539,14 +592,11 @@ __device__ __forceinline__ void residual_cell(const TopoView& t, const R* __rest
     case 2: beta = 1.0 / 3.0; alpha_next = 1.0; break;
     default: beta = 1.0 / 6.0; alpha_next = 0.0; break;
   }
-  // dt/V as the reference rounds it (div_by_recip returns the IEEE quotient);
-  // the mixed form multiplies by 1/V.
-  const double dtv = std::is_same<R, double>::value ? div_by_recip(dt, t.vol[c], t.vinv[c]) : dt * t.vinv[c];
   double ut[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
     // 0.0 + x as in apply_cell_flux (it only normalises a -0 result).
-    const double r = std::is_same<R, double>::value ? 0.0 + dtv * acc[k] : dtv * acc[k];
+    const double r = cell_flux ? acc[k] : std::is_same<R, double>::value ? 0.0 + dtv * acc[k] : dtv * acc[k];
     if (res_out) res_out[k * C + c] = r;
     if (stage == 0) {
       const double un = Un[k * C + c];
@@ -593,9 +643,9 @@ template <class R>
 __global__ void __launch_bounds__(kCellBlock) k_residual(TopoView t, const R* __restrict__ fflux,
                                                          double* __restrict__ Un, double* __restrict__ Unp1,
                                                          R* __restrict__ W, double* __restrict__ res_out, double dt,
-                                                         int stage) {
+                                                         int stage, bool cell_flux) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c < t.C) residual_cell<R>(t, fflux, Un, Unp1, W, res_out, dt, stage, c);
+  if (c < t.C) residual_cell<R>(t, fflux, Un, Unp1, W, res_out, dt, stage, cell_flux, c);
 }
 
 // ---- batched kernels: persistent grid over chunks of (segment, first item) ----
@@ -641,13 +691,14 @@ __global__ void __launch_bounds__(256) kb_bc_flux(const Segment<R>* __restrict__
 
 template <class R>
 __global__ void __launch_bounds__(256) kb_residual(const Segment<R>* __restrict__ segs, const int2* __restrict__ chunks,
-                                                   const int* __restrict__ nchunks, int stage) {
+                                                   const int* __restrict__ nchunks, int stage, bool cell_flux) {
   const int n = *nchunks;
   for (int ch = blockIdx.x; ch < n; ch += gridDim.x) {
     const int2 cs = chunks[ch];
     const Segment<R>& sg = segs[cs.x];
     const int c = cs.y + threadIdx.x;
-    if (c < sg.t.C) residual_cell<R>(sg.t, sg.b.fflux, sg.s.Un, sg.s.Unp1, sg.b.W, sg.s.res, sg.dt, stage, c);
+    if (c < sg.t.C)
+      residual_cell<R>(sg.t, sg.b.fflux, sg.s.Un, sg.s.Unp1, sg.b.W, sg.s.res, sg.dt, stage, cell_flux, c);
   }
 }
 
@@ -707,7 +758,7 @@ cudaError_t launch_stage_impl(const TopoView& t, const GeomView<R>& g, const Pat
     k_bc_flux<R><<<blocks_for(t.Fb, kFaceBlock), kFaceBlock, 0, stream>>>(t, g, b.W, cfg.transport, inflow, b.fflux);
   }
   if (kernels & kResidual)
-    k_residual<R><<<gc, kCellBlock, 0, stream>>>(t, b.fflux, s.Un, s.Unp1, b.W, s.res, cfg.dt, stage);
+    k_residual<R><<<gc, kCellBlock, 0, stream>>>(t, b.fflux, s.Un, s.Unp1, b.W, s.res, cfg.dt, stage, cfg.cell_flux);
   return cudaGetLastError();
 }
 
@@ -740,7 +791,7 @@ cudaError_t launch_batch_stage_impl(const PathConfig& cfg, const Segment<R>* seg
   }
   if (kernels & kBcFlux) kb_bc_flux<R><<<bl.grid[2], bl.block[2], 0, stream>>>(segs, bl.chunks[2], bl.nchunks + 2, tr);
   if (kernels & kResidual)
-    kb_residual<R><<<bl.grid[3], bl.block[3], 0, stream>>>(segs, bl.chunks[3], bl.nchunks + 3, stage);
+    kb_residual<R><<<bl.grid[3], bl.block[3], 0, stream>>>(segs, bl.chunks[3], bl.nchunks + 3, stage, cfg.cell_flux);
   return cudaGetLastError();
 }
 

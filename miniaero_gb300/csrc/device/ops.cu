@@ -81,7 +81,8 @@ __device__ __forceinline__ double make_double(uint64_t r, int e0, int span, bool
 
 // div_by_recip against the IEEE quotient on generated operand pairs.
 // mode 0: random a and b; 1: b with an all-ones significand (possibly a few
-// bits cleared); 2: quotients close to a rounding midpoint.
+// bits cleared); 2: quotients close to a rounding midpoint; 5: tiny,
+// subnormal and zero numerators (3 and 4 check the float conversions).
 __global__ void k_check_division(int mode, unsigned long long n, unsigned long long seed,
                                  unsigned long long* mismatches, double* example) {
   const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
@@ -135,10 +136,17 @@ __global__ void k_check_division(int mode, unsigned long long n, unsigned long l
       }
       continue;
     }
+    if (mode == 5) {
+      // Numerators from the subnormal range up to 2^-880 (quotients near and
+      // below the underflow threshold), and signed zeros.
+      const uint64_t e = r2 % 144u;  // biased exponents 0..143
+      a = __longlong_as_double(static_cast<long long>((r1 & 0x800FFFFFFFFFFFFFull) | (e << 52)));
+      if ((r3 & 63u) == 0u) a = ((r3 >> 6) & 1u) ? -0.0 : 0.0;
+    }
     const double y = 1.0 / b;
     const double q = div_by_recip(a, b, y);
     const double ref = a / b;
-    if (__double_as_longlong(q) != __double_as_longlong(ref) && !(q == 0.0 && ref == 0.0)) {
+    if (__double_as_longlong(q) != __double_as_longlong(ref)) {  // zeros included, with their sign
       if (atomicAdd(mismatches, 1ull) == 0ull) {
         example[0] = a;
         example[1] = b;

@@ -32,17 +32,47 @@ template <> __device__ __forceinline__ float dabs<float>(float x) { return fabsf
 // q1 = RN(q0 + RN(a - b*q0)*y) is faithful (error <= 1/2 ulp + O(2^-104));
 // by Markstein's theorem (y correctly rounded, q1 faithful, binary64, no
 // underflow or overflow) RN(q1 + (a - b*q1)*y) is the correctly rounded
-// quotient. 1 multiply + 4 FMAs instead of a full division. A zero quotient
-// may carry the opposite sign to a/b; every use below adds the result to an
-// accumulator that starts at +0, where the sign of a zero term never shows.
+// quotient. 1 multiply + 4 FMAs instead of a full division. The residuals
+// a - b*q are exact only while their lowest bit, about ulp(b)*ulp(q), is not
+// below the subnormal spacing, and the argument wants a normal RN(1/b): when
+// the exponents of q and b add up to less than -960 (quotients near or in the
+// subnormal range), q is not finite, or b is subnormal or >= 2^1022, the IEEE
+// division is taken instead (rare; integer tests decide). A zero numerator
+// returns a*y, which already is the IEEE zero quotient with its sign.
 __device__ __forceinline__ double div_by_recip(double a, double b, double y) {
   double q = a * y;
+  const uint32_t eq = (static_cast<uint32_t>(__double2hiint(q)) >> 20) & 0x7FFu;
+  const uint32_t eb = (static_cast<uint32_t>(__double2hiint(b)) >> 20) & 0x7FFu;
+  if (eq + eb < 1086u || eq == 0x7FFu || eb - 1u > 2043u) {
+    const uint32_t ah = static_cast<uint32_t>(__double2hiint(a)) & 0x7FFFFFFFu;
+    if ((ah | static_cast<uint32_t>(__double2loint(a))) == 0u) return q;
+    return a / b;
+  }
   double r = fma(-q, b, a);
   q = fma(r, y, q);
   r = fma(-q, b, a);
   return fma(r, y, q);
 }
 __device__ __forceinline__ float div_by_recip(float a, float /*b*/, float y) { return a * y; }
+
+// The reciprocal-method quotient without the IEEE fallback, for hot loops
+// that handle the rare cases out of line: `inexact` is set when the quotient
+// may differ from a/b (the conditions of div_by_recip, with zero numerators
+// excluded: their quotient is a zero of either sign, and the callers only
+// add it to sums that start at +0, where the sign of a zero never shows).
+__device__ __forceinline__ double div_by_recip_flag(double a, double b, double y, bool& inexact) {
+  double q = a * y;
+  const uint32_t eq = (static_cast<uint32_t>(__double2hiint(q)) >> 20) & 0x7FFu;
+  const uint32_t eb = (static_cast<uint32_t>(__double2hiint(b)) >> 20) & 0x7FFu;
+  const uint32_t ah = static_cast<uint32_t>(__double2hiint(a)) & 0x7FFFFFFFu;
+  const bool range = (eq + eb < 1086u) | (eq == 0x7FFu) | (eb - 1u > 2043u);
+  inexact |= range & ((ah | static_cast<uint32_t>(__double2loint(a))) != 0u);
+  double r = fma(-q, b, a);
+  q = fma(r, y, q);
+  r = fma(-q, b, a);
+  return fma(r, y, q);
+}
+__device__ __forceinline__ float div_by_recip_flag(float a, float /*b*/, float y, bool& /*inexact*/) { return a * y; }
 
 // float -> double by bit manipulation on the integer pipe (the FP64 pipe is
 // the residual kernel's bottleneck): exact for normal floats, zeros, inf and

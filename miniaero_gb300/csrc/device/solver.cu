@@ -53,6 +53,8 @@ struct Arena {
 
 struct ma_mesh {
   dev::TopoView topo;
+  dev::TopoView topo_cf;     // topo with the CELL_FLUX lists (MA_MESH_CELL_FLUX)
+  bool has_cell_flux = false;
   dev::GeomView<double> g64;
   dev::GeomView<float> g32;
   void* dmem = nullptr;
@@ -62,6 +64,7 @@ struct ma_mesh {
 
 struct ma_solver {
   ma_mesh* mesh = nullptr;
+  dev::TopoView topo;  // the mesh's lists in the gather order of the options
   ma_options opts;
   dev::PathConfig cfg;
   bool mixed = false;
@@ -134,8 +137,12 @@ inline int type_rank(int type) {
 
 }  // namespace
 
-extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
+extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) { return ma_mesh_upload_ex(v, 0, out); }
+
+extern "C" ma_status ma_mesh_upload_ex(const ma_mesh_view* v, int32_t flags, ma_mesh** out) {
   if (!out) return set_error(MA_EINVAL, "ma_mesh_upload: out is null");
+  if (flags & ~MA_MESH_CELL_FLUX) return set_error(MA_EINVAL, "ma_mesh_upload_ex: unknown flags");
+  const bool cell_flux = (flags & MA_MESH_CELL_FLUX) != 0;
   *out = nullptr;
   ma_status st = validate_view(v);
   if (st != MA_OK) return st;
@@ -315,6 +322,37 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
             push(csr_flux, nf, v->bc[b].conn[2 * i], ((bc_base[b] + i) << 1) | 1, 0, false);
     if (overflow) return set_error(MA_EINVAL, "a cell has more than 6 faces");
 
+    // CELL_FLUX lists (MA_MESH_CELL_FLUX): each cell's faces in element-local
+    // slot order (flux_index, Faces.h:109-110), the order in which the
+    // reference's -DCELL_FLUX build sums its per-slot storage (GreenGauss.h:
+    // 244-269, Flux.h:188-229); one list serves the gradient and the residual.
+    std::vector<int32_t> cf_grad, cf_nbr, cf_flux;
+    if (cell_flux) {
+      cf_grad.assign(K * C, -1);
+      cf_nbr.assign(K * C, -1);
+      auto put = [&](int32_t cell, int32_t slot, int32_t code, int32_t nbr) {
+        if (slot < 0 || slot >= static_cast<int32_t>(K)) return false;
+        int32_t& dst = cf_grad[static_cast<size_t>(slot) * C + cell];
+        if (dst != -1) return false;
+        dst = code;
+        cf_nbr[static_cast<size_t>(slot) * C + cell] = nbr;
+        return true;
+      };
+      bool ok = v->internal.nfaces == 0 || v->internal.flux_index;
+      for (int b = 0; b < v->nbc; ++b) ok = ok && (v->bc[b].nfaces == 0 || v->bc[b].flux_index);
+      if (!ok) return set_error(MA_EINVAL, "MA_MESH_CELL_FLUX needs every face set's flux_index");
+      for (int32_t i = 0; i < Fi && ok; ++i) {
+        const int32_t g = gpu_of_internal[i];
+        const int32_t L = v->internal.conn[2 * i], R = v->internal.conn[2 * i + 1];
+        ok = put(L, v->internal.flux_index[2 * i], (g << 1) | 1, R) && put(R, v->internal.flux_index[2 * i + 1], g << 1, L);
+      }
+      for (int b = 0; b < v->nbc && ok; ++b)
+        for (int32_t i = 0; i < v->bc[b].nfaces && ok; ++i)
+          ok = put(v->bc[b].conn[2 * i], v->bc[b].flux_index[2 * i], ((bc_base[b] + i) << 1) | 1, -1);
+      if (!ok) return set_error(MA_EINVAL, "flux_index out of range or repeated within a cell");
+      cf_flux = cf_grad;  // residual order: plain slot order
+    }
+
     // Axis-aligned cells: every face area vector has exactly one nonzero
     // component and each axis owns two faces. A gradient component (k, d)
     // then receives nonzero terms only from the two d-faces; the other terms
@@ -331,11 +369,10 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
       };
       for (int32_t c = 0; c < C; ++c) {
         if (ng[c] != K) continue;
-        int32_t codes[6], nbrs[6], axes[6], count[3] = {0, 0, 0};
+        int32_t codes[6], axes[6], count[3] = {0, 0, 0};
         bool ok = true;
         for (size_t s2 = 0; s2 < K && ok; ++s2) {
           codes[s2] = csr_grad[s2 * C + c];
-          nbrs[s2] = csr_nbr[s2 * C + c];
           axes[s2] = axis_of(codes[s2] >> 1);
           if (axes[s2] < 0 || ++count[axes[s2]] > 2) ok = false;
         }
@@ -350,14 +387,25 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
           for (int d = 0; d < 3; ++d)
             if (d != axes[s2] && geo[(base + d) * static_cast<size_t>(F) + g] != 0.0) aligned = false;
         }
-        size_t out = 0;
-        for (int d = 0; d < 3; ++d)
-          for (size_t s2 = 0; s2 < K; ++s2)
-            if (axes[s2] == d) {
-              csr_grad[out * C + c] = codes[s2];
-              csr_nbr[out * C + c] = nbrs[s2];
-              ++out;
-            }
+        // Group a list by axis, keeping its order within each axis.
+        auto regroup = [&](std::vector<int32_t>& grad, std::vector<int32_t>& nbr) {
+          int32_t cs[6], ns[6], as[6];
+          for (size_t s2 = 0; s2 < K; ++s2) {
+            cs[s2] = grad[s2 * C + c];
+            ns[s2] = nbr[s2 * C + c];
+            as[s2] = axis_of(cs[s2] >> 1);
+          }
+          size_t out = 0;
+          for (int d = 0; d < 3; ++d)
+            for (size_t s2 = 0; s2 < K; ++s2)
+              if (as[s2] == d) {
+                grad[out * C + c] = cs[s2];
+                nbr[out * C + c] = ns[s2];
+                ++out;
+              }
+        };
+        regroup(csr_grad, csr_nbr);
+        if (cell_flux) regroup(cf_grad, cf_nbr);
         axis_cell[c] = aligned ? 3 : 1;
       }
     }
@@ -378,6 +426,11 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
       float* vol32 = a.take<float>(C);
       double* vinv64 = a.take<double>(C);
       float* vinv32 = a.take<float>(C);
+      if (cell_flux) {
+        m.topo_cf.csr_grad = a.take<int32_t>(K * C);
+        m.topo_cf.csr_nbr = a.take<int32_t>(K * C);
+        m.topo_cf.csr_flux = a.take<int32_t>(K * C);
+      }
       auto assign = [&](auto& gv, auto* base, auto* vol, auto* vinv) {
         gv.vol = vol;
         gv.vinv = vinv;
@@ -408,6 +461,14 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
     m->topo.Fb = Fb;
     m->topo.F = F;
     for (int r = 0; r < 4; ++r) m->topo.nbc_type[r] = nbc_type[r];
+    if (cell_flux) {  // same topology and flags, lists in slot order
+      const dev::TopoView lists = m->topo_cf;
+      m->topo_cf = m->topo;
+      m->topo_cf.csr_grad = lists.csr_grad;
+      m->topo_cf.csr_nbr = lists.csr_nbr;
+      m->topo_cf.csr_flux = lists.csr_flux;
+      m->has_cell_flux = true;
+    }
 
     std::unique_ptr<float[]> geo32(new float[geo_size]);
     miniaero::parallel_for(geo_size, [&](size_t b, size_t e) {
@@ -429,6 +490,11 @@ extern "C" ma_status ma_mesh_upload(const ma_mesh_view* v, ma_mesh** out) {
     if (e == cudaSuccess) e = copy(m->topo.csr_grad, csr_grad.data(), sizeof(int32_t) * csr_grad.size());
     if (e == cudaSuccess) e = copy(m->topo.csr_nbr, csr_nbr.data(), sizeof(int32_t) * csr_nbr.size());
     if (e == cudaSuccess) e = copy(m->topo.csr_flux, csr_flux.data(), sizeof(int32_t) * csr_flux.size());
+    if (cell_flux) {
+      if (e == cudaSuccess) e = copy(m->topo_cf.csr_grad, cf_grad.data(), sizeof(int32_t) * cf_grad.size());
+      if (e == cudaSuccess) e = copy(m->topo_cf.csr_nbr, cf_nbr.data(), sizeof(int32_t) * cf_nbr.size());
+      if (e == cudaSuccess) e = copy(m->topo_cf.csr_flux, cf_flux.data(), sizeof(int32_t) * cf_flux.size());
+    }
     if (e == cudaSuccess) e = copy(m->topo.axis_cell, axis_cell.data(), axis_cell.size());
     if (e == cudaSuccess && Fi > 0) e = copy(m->topo.fclass, fclass_dev.data(), fclass_dev.size());
     if (e == cudaSuccess) e = copy(m->g64.fn, geo, sizeof(double) * geo_size);
@@ -452,6 +518,10 @@ namespace miniaero {
 size_t mesh_cells(const ma_mesh* m) { return static_cast<size_t>(m->topo.C); }
 size_t mesh_faces(const ma_mesh* m) { return static_cast<size_t>(m->topo.F); }
 dev::TopoView mesh_topo(const ma_mesh* m) { return m->topo; }
+dev::TopoView mesh_topo(const ma_mesh* m, int gather) {
+  return gather == MA_GATHER_CELL_FLUX ? m->topo_cf : m->topo;
+}
+bool mesh_has_cell_flux(const ma_mesh* m) { return m->has_cell_flux; }
 template <>
 dev::GeomView<double> mesh_geom<double>(const ma_mesh* m) { return m->g64; }
 template <>
@@ -479,9 +549,9 @@ ma_status capture_step_graph(ma_solver* s) {
   cudaError_t e = cudaSuccess;
   for (int stage = 0; stage < 4 && e == cudaSuccess; ++stage) {
     if (s->mixed)
-      e = dev::launch_stage<float>(s->mesh->topo, s->mesh->g32, s->cfg, s->st, s->b32, stage, s->stream);
+      e = dev::launch_stage<float>(s->topo, s->mesh->g32, s->cfg, s->st, s->b32, stage, s->stream);
     else
-      e = dev::launch_stage<double>(s->mesh->topo, s->mesh->g64, s->cfg, s->st, s->b64, stage, s->stream);
+      e = dev::launch_stage<double>(s->topo, s->mesh->g64, s->cfg, s->st, s->b64, stage, s->stream);
   }
   cudaError_t e2 = cudaStreamEndCapture(s->stream, &g);
   if (e != cudaSuccess || e2 != cudaSuccess) {
@@ -506,9 +576,14 @@ extern "C" ma_status ma_solver_create(ma_mesh* mesh, const ma_options* o, ma_sol
   if (o->viscosity_model == MA_VISC_CONSTANT && !(o->mu >= 0.0 && o->prandtl > 0.0))
     return set_error(MA_EINVAL, "constant viscosity needs mu >= 0 and prandtl > 0");
   if (!(o->cfl > 0.0) && !(o->dt > 0.0)) return set_error(MA_EINVAL, "dt must be > 0 (or cfl > 0)");
+  if (o->gather != MA_GATHER_ATOMICS && o->gather != MA_GATHER_CELL_FLUX) return set_error(MA_EINVAL, "bad gather");
+  if (o->gather == MA_GATHER_CELL_FLUX && !mesh->has_cell_flux)
+    return set_error(MA_EINVAL, "gather cell_flux needs a mesh uploaded with MA_MESH_CELL_FLUX");
   ma_solver* s = new (std::nothrow) ma_solver;
   if (!s) return set_error(MA_ENOMEM, "ma_solver_create: out of host memory");
   s->mesh = mesh;
+  s->topo = o->gather == MA_GATHER_CELL_FLUX ? mesh->topo_cf : mesh->topo;
+  s->cfg.cell_flux = o->gather == MA_GATHER_CELL_FLUX;
   s->opts = *o;
   s->mixed = o->precision == MA_PREC_MIXED;
   s->cfg.second_order = o->second_order_space != 0;
@@ -574,7 +649,7 @@ namespace {
 
 // Copies U (AOS or SOA host layout) into the device SOA array.
 ma_status upload_state(ma_solver* s, const double* U, int32_t layout) {
-  const size_t C = s->mesh->topo.C;
+  const size_t C = s->topo.C;
   if (layout == MA_LAYOUT_SOA) {
     MA_CUDA_TRY(cudaMemcpyAsync(s->st.Un, U, sizeof(double) * 5 * C, cudaMemcpyHostToDevice, s->stream));
   } else if (layout == MA_LAYOUT_AOS) {
@@ -590,7 +665,7 @@ ma_status upload_state(ma_solver* s, const double* U, int32_t layout) {
 }
 
 ma_status download(ma_solver* s, const double* src, double* U, int32_t layout) {
-  const size_t C = s->mesh->topo.C;
+  const size_t C = s->topo.C;
   if (layout == MA_LAYOUT_SOA) {
     MA_CUDA_TRY(cudaMemcpyAsync(U, src, sizeof(double) * 5 * C, cudaMemcpyDeviceToHost, s->stream));
     MA_CUDA_TRY(cudaStreamSynchronize(s->stream));
@@ -613,10 +688,12 @@ extern "C" ma_status ma_solver_set_state(ma_solver* s, const double* U, int32_t 
   MA_CUDA_TRY(cudaSetDevice(s->mesh->device));
   ma_status st = upload_state(s, U, layout);
   if (st != MA_OK) return st;
-  const dev::TopoView& t = s->mesh->topo;
+  const dev::TopoView& t = s->topo;
   if (s->opts.cfl > 0.0) {
     MA_CUDA_TRY(cudaMemsetAsync(s->dscratch, 0xff, sizeof(unsigned long long), s->stream));
-    MA_CUDA_TRY(dev::launch_cfl(t, s->mesh->g64, s->st.Un, s->dscratch, s->stream));
+    // The CFL sum runs over the mesh's default lists whatever the gather
+    // order, so dt does not depend on it.
+    MA_CUDA_TRY(dev::launch_cfl(s->mesh->topo, s->mesh->g64, s->st.Un, s->dscratch, s->stream));
     unsigned long long bits = 0;
     MA_CUDA_TRY(cudaMemcpyAsync(&bits, s->dscratch, sizeof(bits), cudaMemcpyDeviceToHost, s->stream));
     MA_CUDA_TRY(cudaStreamSynchronize(s->stream));
@@ -639,7 +716,7 @@ extern "C" ma_status ma_solver_set_state(ma_solver* s, const double* U, int32_t 
 
 extern "C" ma_status ma_solver_init_state(ma_solver* s, const ma_host_mesh* hm) {
   if (!s || !hm) return set_error(MA_EINVAL, "ma_solver_init_state: null argument");
-  std::vector<double> U(5 * static_cast<size_t>(s->mesh->topo.C));
+  std::vector<double> U(5 * static_cast<size_t>(s->topo.C));
   ma_status st = ma_host_initial_state(hm, &s->opts, U.data());
   if (st != MA_OK) return st;
   return ma_solver_set_state(s, U.data(), MA_LAYOUT_AOS);
@@ -679,7 +756,7 @@ extern "C" ma_status ma_solver_profile_steps(ma_solver* s, int32_t nsteps, doubl
   if (!s->state_set) return set_error(MA_ESTATE, "solver state has not been set");
   MA_CUDA_TRY(cudaSetDevice(s->mesh->device));
   for (int k = 0; k < MA_PROFILE_KINDS; ++k) { kernel_ms[k] = 0.0; kernel_launches[k] = 0; }
-  const dev::TopoView& t = s->mesh->topo;
+  const dev::TopoView& t = s->topo;
   const unsigned bits[MA_PROFILE_KINDS] = {dev::kSweep1, dev::kInternalFlux, dev::kBcFlux, dev::kResidual};
   bool present[MA_PROFILE_KINDS] = {s->cfg.second_order || s->cfg.viscous, t.Fi > 0, t.Fb > 0, true};
   std::vector<cudaEvent_t> ev;
@@ -733,7 +810,7 @@ extern "C" double ma_solver_dt(const ma_solver* s) { return s ? s->cfg.dt : 0.0;
 extern "C" int64_t ma_solver_steps_done(const ma_solver* s) { return s ? s->steps_done : 0; }
 
 extern "C" int32_t ma_solver_launches_per_step(const ma_solver* s) {
-  return s ? 4 * dev::launches_per_stage(s->cfg, s->mesh->topo) : 0;
+  return s ? 4 * dev::launches_per_stage(s->cfg, s->topo) : 0;
 }
 
 extern "C" ma_status ma_solver_set_dt(ma_solver* s, double dt) {
@@ -751,7 +828,7 @@ extern "C" ma_status ma_solver_check_state(ma_solver* s, int64_t* bad_cell) {
   if (bad_cell) *bad_cell = -1;
   MA_CUDA_TRY(cudaSetDevice(s->mesh->device));
   MA_CUDA_TRY(cudaMemsetAsync(s->dscratch, 0xff, sizeof(unsigned long long), s->stream));
-  MA_CUDA_TRY(dev::launch_check_state(s->mesh->topo.C, s->st.Un, s->dscratch, s->stream));
+  MA_CUDA_TRY(dev::launch_check_state(s->topo.C, s->st.Un, s->dscratch, s->stream));
   unsigned long long first = 0;
   MA_CUDA_TRY(cudaMemcpyAsync(&first, s->dscratch, sizeof(first), cudaMemcpyDeviceToHost, s->stream));
   MA_CUDA_TRY(cudaStreamSynchronize(s->stream));
@@ -841,7 +918,7 @@ extern "C" ma_status ma_op_limiter(int32_t n, int32_t kind, const double* dumax,
 
 extern "C" ma_status ma_debug_check_division(int32_t mode, uint64_t n, uint64_t seed, uint64_t* mismatches,
                                              double* example) {
-  if (!mismatches || !example || mode < 0 || mode > 4) return set_error(MA_EINVAL, "ma_debug_check_division: bad arguments");
+  if (!mismatches || !example || mode < 0 || mode > 5) return set_error(MA_EINVAL, "ma_debug_check_division: bad arguments");
   DevBufs b;
   double* dex;
   MA_CUDA_TRY(b.in(nullptr, 3, &dex));

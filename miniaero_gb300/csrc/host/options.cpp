@@ -41,6 +41,7 @@ extern "C" void ma_options_default(ma_options* o) {
   o->inflow_state[3] = 0.0; o->inflow_state[4] = 343750.0;
   for (int i = 0; i < 6; ++i) o->bc_override[i] = -1;
   o->keep_residual = 0;
+  o->gather = MA_GATHER_ATOMICS;
 }
 
 namespace {
@@ -110,6 +111,11 @@ extern "C" ma_status ma_options_read(const char* path, ma_options* o) {
       std::string side, type; in >> side >> type;
       const int si = side_index(side), bi = bc_index(type);
       if (si < 0 || bi < 0) ok = false; else o->bc_override[si] = bi;
+    } else if (key == "gather") {
+      std::string v; in >> v;
+      if (v == "atomics") o->gather = MA_GATHER_ATOMICS;
+      else if (v == "cell_flux") o->gather = MA_GATHER_CELL_FLUX;
+      else ok = false;
     } else if (key == "keep_residual") {
       in >> o->keep_residual;
     } else if (key == "checkpoint" || key == "restart") {

@@ -113,10 +113,11 @@ size_t dry_member_bytes(const ma_server* s, const ma_request& r) {
   return static_cast<size_t>(C) * (80 + 25 * w) + static_cast<size_t>(F) * 5 * w + 6 * 256;
 }
 
-size_t dry_mesh_bytes(const ma_request& r) {
+size_t dry_mesh_bytes(const ma_server* s, const ma_request& r) {
   int64_t C, F;
   box_counts(r, C, F);
-  return static_cast<size_t>(C) * 100 + static_cast<size_t>(F) * 237 + 16 * 256;
+  const size_t cell_flux = s->physics.gather == MA_GATHER_CELL_FLUX ? 72 : 0;  // slot-order lists
+  return static_cast<size_t>(C) * (100 + cell_flux) + static_cast<size_t>(F) * 237 + 19 * 256;
 }
 
 MeshKey key_of(const ma_request& r) {
@@ -161,14 +162,14 @@ ma_status ensure_mesh(ma_server* s, Request& q, CachedMesh** out) {
   }
   CachedMesh cm;
   if (s->dry) {
-    cm.bytes = dry_mesh_bytes(q.req);
+    cm.bytes = dry_mesh_bytes(s, q.req);
   } else {
     ma_options o = options_of(s, q.req);
     ma_status st = ma_host_mesh_build(&o, &cm.host);
     if (st != MA_OK) return st;
     ma_mesh_view v;
     ma_host_mesh_view(cm.host, &v);
-    st = ma_mesh_upload(&v, &cm.dev);
+    st = ma_mesh_upload_ex(&v, s->physics.gather == MA_GATHER_CELL_FLUX ? MA_MESH_CELL_FLUX : 0, &cm.dev);
     if (st != MA_OK) {
       ma_host_mesh_free(cm.host);
       return st;
@@ -216,7 +217,7 @@ void admit(ma_server* s) {
       if (s->max_running_cells > 0 && s->running_cells > 0 && s->running_cells + C > s->max_running_cells) return;
     }
     const bool cached = s->meshes.count(q.key) != 0;
-    const size_t mesh_need = cached ? 0 : dry_mesh_bytes(q.req);
+    const size_t mesh_need = cached ? 0 : dry_mesh_bytes(s, q.req);
     size_t member_need = dry_member_bytes(s, q.req);
     if (!make_room(s, mesh_need + member_need)) return;  // wait for memory
     CachedMesh* cm = nullptr;
@@ -423,7 +424,7 @@ extern "C" ma_status ma_server_submit(ma_server* s, const ma_request* r, int64_t
   q.key = key_of(*r);
   q.t_submit = ns_since(s->t0);
   // A request that cannot fit even in an empty server is rejected now.
-  if (dry_member_bytes(s, *r) + dry_mesh_bytes(*r) > s->budget) {
+  if (dry_member_bytes(s, *r) + dry_mesh_bytes(s, *r) > s->budget) {
     q.state = MA_REQ_FAILED;
     q.error = MA_EBUDGET;
     q.message = "request larger than the device-memory budget";
@@ -446,7 +447,7 @@ extern "C" ma_status ma_server_preload_mesh(ma_server* s, const ma_request* r) {
   q.req = *r;
   q.key = key_of(*r);
   CachedMesh* cm = nullptr;
-  const size_t need = s->meshes.count(q.key) ? 0 : dry_mesh_bytes(*r);
+  const size_t need = s->meshes.count(q.key) ? 0 : dry_mesh_bytes(s, *r);
   if (need && !make_room(s, need)) return set_error(MA_EBUDGET, "mesh does not fit the budget");
   ma_status st = ensure_mesh(s, q, &cm);
   if (st == MA_OK) cm->last_used = ns_since(s->t0);

@@ -19,7 +19,8 @@ P_f64 = ctypes.POINTER(ctypes.c_double)
 
 class oracle_faces(ctypes.Structure):
     _fields_ = [("nfaces", ctypes.c_int), ("type", ctypes.c_int), ("conn", P_i32), ("coords", P_f64),
-                ("normal", P_f64), ("tangent", P_f64), ("binormal", P_f64), ("permutation", P_i32)]
+                ("normal", P_f64), ("tangent", P_f64), ("binormal", P_f64), ("permutation", P_i32),
+                ("flux_index", P_i32)]
 
 
 class oracle_mesh(ctypes.Structure):
@@ -30,7 +31,8 @@ class oracle_mesh(ctypes.Structure):
 class oracle_options(ctypes.Structure):
     _fields_ = [("second_order", ctypes.c_int), ("viscous", ctypes.c_int), ("limiter", ctypes.c_int),
                 ("viscosity_model", ctypes.c_int), ("mu", ctypes.c_double), ("prandtl", ctypes.c_double),
-                ("dt", ctypes.c_double), ("nsteps", ctypes.c_int), ("inflow_state", ctypes.c_double * 5)]
+                ("dt", ctypes.c_double), ("nsteps", ctypes.c_int), ("inflow_state", ctypes.c_double * 5),
+                ("cell_flux", ctypes.c_int)]
 
 
 _lib = None
@@ -81,6 +83,8 @@ class OracleMesh:
             f.tangent = _p(fs.tangent, P_f64)
             f.binormal = _p(fs.binormal, P_f64)
             f.permutation = _p(fs.permutation, P_i32)
+            fi = getattr(fs, "flux_index", None)
+            f.flux_index = _p(fi, P_i32) if fi is not None else ctypes.cast(None, P_i32)
             return f
 
         self.bc = (oracle_faces * max(1, len(md.bc)))()
@@ -108,6 +112,7 @@ def _c_options(options, nsteps=None, dt=None):
     o.nsteps = int(options.ntimesteps if nsteps is None else nsteps)
     for k in range(5):
         o.inflow_state[k] = options.inflow_state[k]
+    o.cell_flux = int(options.gather == 1)  # MA_GATHER_CELL_FLUX
     return o
 
 

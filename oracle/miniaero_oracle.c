@@ -271,7 +271,16 @@ typedef struct {
   double *smin, *smax; /* [C*5] stored and stencil min/max (ATOMICS layout) */
   double *slim;        /* [C*5] stored limiter */
   double *lim;         /* [C*5] limiter */
+  /* CELL_FLUX storage, one entry per element-local face slot (Cells.h:70-73) */
+  int cf;
+  double *cf_flux;     /* [C*6*5] */
+  double *cf_grad;     /* [C*6*15] */
+  double *cf_min, *cf_max, *cf_lim;  /* [C*6*5] */
 } ostate;
+
+#define NSLOTS 6  /* Hexa8 faces per cell */
+static inline size_t slot5(int c, int slot) { return ((size_t)c * NSLOTS + (size_t)slot) * 5; }
+static inline size_t slot15(int c, int slot) { return ((size_t)c * NSLOTS + (size_t)slot) * 15; }
 
 #define PFOR _Pragma("omp parallel for schedule(static) if(s->par) num_threads(s->nt)")
 
@@ -292,6 +301,11 @@ static void zero_cell_flux(ostate* s) {
       s->cell_flux[5 * i + k] = 0.0;
       for (int d = 0; d < 3; ++d) s->cell_grad[15 * i + 3 * k + d] = 0.0;
     }
+    if (s->cf)
+      for (int slot = 0; slot < NSLOTS; ++slot) {
+        for (int k = 0; k < 5; ++k) s->cf_flux[slot5(i, slot) + k] = 0.0;
+        for (int j = 0; j < 15; ++j) s->cf_grad[slot15(i, slot) + j] = 0.0;
+      }
   }
 }
 
@@ -313,8 +327,13 @@ static void green_gauss(ostate* s) {
       const double fn = f->normal[3 * i + d];
       for (int k = 0; k < 5; ++k) {
         const double g = 0.5 * (pl[k] + pr[k]) * fn;
-        atomic_add_d(&s->cell_grad[15 * L + 3 * k + d], g / vl, s->par);
-        atomic_add_d(&s->cell_grad[15 * R + 3 * k + d], -g / vr, s->par);
+        if (s->cf) {  /* GreenGauss.h:129-132 */
+          s->cf_grad[slot15(L, f->flux_index[2 * i]) + 3 * k + d] = g / vl;
+          s->cf_grad[slot15(R, f->flux_index[2 * i + 1]) + 3 * k + d] = -g / vr;
+        } else {
+          atomic_add_d(&s->cell_grad[15 * L + 3 * k + d], g / vl, s->par);
+          atomic_add_d(&s->cell_grad[15 * R + 3 * k + d], -g / vr, s->par);
+        }
       }
     }
   }
@@ -328,7 +347,12 @@ static void green_gauss(ostate* s) {
       for (int k = 0; k < 5; ++k)
         for (int d = 0; d < 3; ++d) g[k][d] = p[k] * bf->normal[3 * i + d];
       for (int k = 0; k < 5; ++k)
-        for (int d = 0; d < 3; ++d) atomic_add_d(&s->cell_grad[15 * c + 3 * k + d], g[k][d] / vol[c], s->par);
+        for (int d = 0; d < 3; ++d) {
+          if (s->cf)  /* GreenGauss.h:211-219 */
+            s->cf_grad[slot15(c, bf->flux_index[2 * i]) + 3 * k + d] = g[k][d] / vol[c];
+          else
+            atomic_add_d(&s->cell_grad[15 * c + 3 * k + d], g[k][d] / vol[c], s->par);
+        }
     }
   }
   const int C = m->ncells;
@@ -336,7 +360,10 @@ static void green_gauss(ostate* s) {
   for (int i = 0; i < C; ++i)                 /* green_gauss_gradient_sum, :244-269 */
     for (int j = 0; j < 15; ++j) {
       double acc = 0;
-      acc += s->cell_grad[15 * i + j];
+      if (s->cf)
+        for (int slot = 0; slot < NSLOTS; ++slot) acc += s->cf_grad[slot15(i, slot) + j];
+      else
+        acc += s->cell_grad[15 * i + j];
       s->grad[15 * i + j] = acc;
     }
 }
@@ -347,8 +374,16 @@ static void min_max(ostate* s) {
   const double* U = s->Utmp;
   const int C = m->ncells;
   PFOR
-  for (int i = 0; i < C; ++i)
-    for (int k = 0; k < 5; ++k) { s->smin[5 * i + k] = 1.0e300; s->smax[5 * i + k] = -1.0e300; }
+  for (int i = 0; i < C; ++i)                  /* initialize_min_max, :227-236 */
+    for (int k = 0; k < 5; ++k) {
+      s->smin[5 * i + k] = 1.0e300;
+      s->smax[5 * i + k] = -1.0e300;
+      if (s->cf)
+        for (int slot = 0; slot < NSLOTS; ++slot) {
+          s->cf_min[slot5(i, slot) + k] = 1.0e300;
+          s->cf_max[slot5(i, slot) + k] = -1.0e300;
+        }
+    }
   const oracle_faces* f = &m->internal;
   PFOR
   for (int ii = 0; ii < f->nfaces; ++ii) {   /* min_max_face<true>, :84-201 */
@@ -360,6 +395,13 @@ static void min_max(ostate* s) {
     for (int k = 0; k < 5; ++k) {
       const double fmin_ = (pr[k] < pl[k]) ? pr[k] : pl[k];
       const double fmax_ = (pr[k] > pl[k]) ? pr[k] : pl[k];
+      if (s->cf) {  /* :191-198 */
+        s->cf_min[slot5(L, f->flux_index[2 * i]) + k] = fmin_;
+        s->cf_max[slot5(L, f->flux_index[2 * i]) + k] = fmax_;
+        s->cf_min[slot5(R, f->flux_index[2 * i + 1]) + k] = fmin_;
+        s->cf_max[slot5(R, f->flux_index[2 * i + 1]) + k] = fmax_;
+        continue;
+      }
       atomic_min_d(&s->smin[5 * L + k], fmin_, s->par);
       atomic_max_d(&s->smax[5 * L + k], fmax_, s->par);
       atomic_min_d(&s->smin[5 * R + k], fmin_, s->par);
@@ -375,12 +417,28 @@ static void min_max(ostate* s) {
       double pl[5];
       oracle_primitives(&U[5 * L], pl);
       for (int k = 0; k < 5; ++k) {
+        if (s->cf) {
+          s->cf_min[slot5(L, bf->flux_index[2 * i]) + k] = pl[k];
+          s->cf_max[slot5(L, bf->flux_index[2 * i]) + k] = pl[k];
+          continue;
+        }
         atomic_min_d(&s->smin[5 * L + k], pl[k], s->par);
         atomic_max_d(&s->smax[5 * L + k], pl[k], s->par);
       }
     }
   }
-  /* gather_min_max (ATOMICS_FLUX) copies stored -> stencil; same buffers here. */
+  /* gather_min_max: ATOMICS_FLUX copies stored -> stencil (same buffers here);
+     CELL_FLUX takes std::min / std::max over the slots in order (:274-279). */
+  if (s->cf) {
+    PFOR
+    for (int i = 0; i < C; ++i)
+      for (int k = 0; k < 5; ++k)
+        for (int slot = 0; slot < NSLOTS; ++slot) {
+          const double a = s->cf_min[slot5(i, slot) + k], b = s->cf_max[slot5(i, slot) + k];
+          s->smin[5 * i + k] = (a < s->smin[5 * i + k]) ? a : s->smin[5 * i + k];
+          s->smax[5 * i + k] = (s->smax[5 * i + k] < b) ? b : s->smax[5 * i + k];
+        }
+  }
 }
 
 static inline double limit_fn(const ostate* s, double dumax, double dumin, double du, double d2) {
@@ -410,8 +468,12 @@ static void limiter(ostate* s) {
   const double* U = s->Utmp;
   const int C = m->ncells;
   PFOR
-  for (int i = 0; i < C; ++i)
-    for (int k = 0; k < 5; ++k) s->slim[5 * i + k] = 1.0;
+  for (int i = 0; i < C; ++i)                  /* initialize_limiter, :306-313 */
+    for (int k = 0; k < 5; ++k) {
+      s->slim[5 * i + k] = 1.0;
+      if (s->cf)
+        for (int slot = 0; slot < NSLOTS; ++slot) s->cf_lim[slot5(i, slot) + k] = 1.0;
+    }
   const oracle_faces* f = &m->internal;
   PFOR
   for (int ii = 0; ii < f->nfaces; ++ii) {
@@ -423,6 +485,11 @@ static void limiter(ostate* s) {
     limiter_side(s, f, i, L, pl, phl);
     limiter_side(s, f, i, R, pr, phr);
     for (int k = 0; k < 5; ++k) {
+      if (s->cf) {  /* :489-497 */
+        s->cf_lim[slot5(L, f->flux_index[2 * i]) + k] = phl[k];
+        s->cf_lim[slot5(R, f->flux_index[2 * i + 1]) + k] = phr[k];
+        continue;
+      }
       atomic_min_d(&s->slim[5 * L + k], phl[k], s->par);
       atomic_min_d(&s->slim[5 * R + k], phr[k], s->par);
     }
@@ -436,12 +503,28 @@ static void limiter(ostate* s) {
       double pl[5], phl[5];
       oracle_primitives(&U[5 * L], pl);
       limiter_side(s, bf, i, L, pl, phl);
-      for (int k = 0; k < 5; ++k) atomic_min_d(&s->slim[5 * L + k], phl[k], s->par);
+      for (int k = 0; k < 5; ++k) {
+        if (s->cf)
+          s->cf_lim[slot5(L, bf->flux_index[2 * i]) + k] = phl[k];
+        else
+          atomic_min_d(&s->slim[5 * L + k], phl[k], s->par);
+      }
     }
   }
   PFOR
-  for (int i = 0; i < C; ++i)                  /* gather_limiter */
-    for (int k = 0; k < 5; ++k) s->lim[5 * i + k] = s->slim[5 * i + k];
+  for (int i = 0; i < C; ++i)                  /* gather_limiter, :336-349 */
+    for (int k = 0; k < 5; ++k) {
+      if (s->cf) {  /* limiter_ starts at 1.0; std::min over the slots in order */
+        double l = 1.0;
+        for (int slot = 0; slot < NSLOTS; ++slot) {
+          const double v = s->cf_lim[slot5(i, slot) + k];
+          l = (v < l) ? v : l;
+        }
+        s->lim[5 * i + k] = l;
+      } else {
+        s->lim[5 * i + k] = s->slim[5 * i + k];
+      }
+    }
 }
 
 /* compute_face_flux (Flux.h:89-180) */
@@ -480,6 +563,11 @@ static void internal_flux(ostate* s) {
       for (int k = 0; k < 5; ++k) flux[k] -= vf[k];
     }
     for (int k = 0; k < 5; ++k) {
+      if (s->cf) {  /* Flux.h:172-178 */
+        s->cf_flux[slot5(L, f->flux_index[2 * i]) + k] = -flux[k];
+        s->cf_flux[slot5(R, f->flux_index[2 * i + 1]) + k] = flux[k];
+        continue;
+      }
       atomic_add_d(&s->cell_flux[5 * L + k], -flux[k], s->par);
       atomic_add_d(&s->cell_flux[5 * R + k], flux[k], s->par);
     }
@@ -542,7 +630,12 @@ static void bc_flux(ostate* s, const oracle_faces* bf) {
       oracle_viscous_flux((const double(*)[3])gf, pf, n, s->o->viscosity_model, s->o->mu, s->o->prandtl, vflux);
       for (int k = 0; k < 5; ++k) contrib[k] = -flux[k] + vflux[k];
     }
-    for (int k = 0; k < 5; ++k) atomic_add_d(&s->cell_flux[5 * c + k], contrib[k], s->par);
+    for (int k = 0; k < 5; ++k) {
+      if (s->cf)  /* Extrapolate_BC.h:94-99 and the other BC functors */
+        s->cf_flux[slot5(c, bf->flux_index[2 * i]) + k] = contrib[k];
+      else
+        atomic_add_d(&s->cell_flux[5 * c + k], contrib[k], s->par);
+    }
   }
 }
 
@@ -554,14 +647,20 @@ static void apply_cell_flux(ostate* s) {
   for (int i = 0; i < C; ++i)
     for (int k = 0; k < 5; ++k) {
       double r = 0.0;
-      r = r + dt / s->m->cell_volumes[i] * s->cell_flux[5 * i + k];
+      if (s->cf)  /* one term per slot, in slot order */
+        for (int slot = 0; slot < NSLOTS; ++slot) r = r + dt / s->m->cell_volumes[i] * s->cf_flux[slot5(i, slot) + k];
+      else
+        r = r + dt / s->m->cell_volumes[i] * s->cell_flux[5 * i + k];
       s->res[5 * i + k] = r;
     }
 }
 
+void oracle_free(oracle_state* h);
+
 struct oracle_state {
   ostate s;
   double* pool;
+  double* cf_pool;
   double* Un;
 };
 
@@ -593,6 +692,21 @@ oracle_state* oracle_create(const oracle_mesh* m, const oracle_options* o, const
   s->grad = q; q += 15 * C;
   memcpy(s->Un, U0, sizeof(double) * 5 * C);
   memcpy(s->Unp1, s->Un, sizeof(double) * 5 * C);    /* copy (TimeSolverExplicitRK4.h:335) */
+  s->cf = o->cell_flux != 0;
+  if (s->cf) {
+    /* CELL_FLUX needs every non-empty face set's flux_index. */
+    int missing = m->internal.nfaces > 0 && !m->internal.flux_index;
+    for (int b = 0; b < m->nbc; ++b) missing |= m->bc[b].nfaces > 0 && !m->bc[b].flux_index;
+    if (missing) { oracle_free(h); return NULL; }
+    h->cf_pool = (double*)calloc(C * NSLOTS * (5 * 4 + 15), sizeof(double));
+    if (!h->cf_pool) { oracle_free(h); return NULL; }
+    double* r = h->cf_pool;
+    s->cf_flux = r; r += NSLOTS * 5 * C;
+    s->cf_min = r; r += NSLOTS * 5 * C;
+    s->cf_max = r; r += NSLOTS * 5 * C;
+    s->cf_lim = r; r += NSLOTS * 5 * C;
+    s->cf_grad = r;
+  }
   return h;
 }
 
@@ -633,6 +747,7 @@ void oracle_get_state(const oracle_state* h, double* U, double* res) {
 void oracle_free(oracle_state* h) {
   if (!h) return;
   free(h->pool);
+  free(h->cf_pool);
   free(h);
 }
 

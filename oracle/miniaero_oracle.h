@@ -30,6 +30,8 @@ typedef struct {
   const double* tangent;    /* [nfaces*3] */
   const double* binormal;   /* [nfaces*3] */
   const int* permutation;   /* [nfaces] iteration order */
+  const int* flux_index;    /* [nfaces*2] element-local face slots of (left, right)
+                               (Faces.h:109-110); read in CELL_FLUX mode only */
 } oracle_faces;
 
 typedef struct {
@@ -51,6 +53,8 @@ typedef struct {
   double dt;
   int nsteps;
   double inflow_state[5];/* conserved inflow state (TimeSolverExplicitRK4.h:218-223) */
+  int cell_flux;         /* 1: the reference's -DCELL_FLUX build (per-slot storage,
+                            gathers in slot order); 0: its default -DATOMICS_FLUX */
 } oracle_options;
 
 /* Advances U (conserved, [ncells*5], in/out) by opts->nsteps RK4 steps.

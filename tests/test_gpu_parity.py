@@ -234,13 +234,15 @@ def test_mixed_flat_plate_density_error(has_gpu):
 
 
 # ---- exact division used by the gradient ------------------------------------------------
-@pytest.mark.parametrize("mode", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("mode", [0, 1, 2, 3, 4, 5])
 def test_reciprocal_division_is_correctly_rounded(has_gpu, mode):
-    """div_by_recip(a, b, RN(1/b)) equals the IEEE quotient a/b (2^28 pairs per
-    mode); mode 3: widen_exact equals the float->double conversion on 2^28
-    random bit patterns (subnormals: signed zero); mode 4: narrow_rn equals
-    the double->float conversion (random patterns, both edges of the float
-    range, exact midpoints and their neighbours)."""
+    """div_by_recip(a, b, RN(1/b)) equals the IEEE quotient a/b bit for bit
+    (2^28 pairs per mode; mode 5: numerators from the subnormal range to
+    2^-880 and signed zeros, where the reciprocal method hands over to the
+    IEEE division); mode 3: widen_exact equals the float->double conversion
+    on 2^28 random bit patterns (subnormals: signed zero); mode 4: narrow_rn
+    equals the double->float conversion (random patterns, both edges of the
+    float range, exact midpoints and their neighbours)."""
     import ctypes
     from miniaero_gb300 import _lib
     mism = ctypes.c_uint64(0)

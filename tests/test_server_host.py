@@ -23,7 +23,7 @@ def sizes(n, mixed=True):
     C = n ** 3
     F = 3 * (n + 1) * n * n
     w = 4 if mixed else 8
-    return C * (80 + 25 * w) + F * 5 * w + 6 * 256, C * 100 + F * 237 + 16 * 256  # member, mesh
+    return C * (80 + 25 * w) + F * 5 * w + 6 * 256, C * 100 + F * 237 + 19 * 256  # member, mesh
 
 
 def test_fifo_admission_under_budget():

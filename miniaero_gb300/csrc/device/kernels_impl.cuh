@@ -598,18 +598,22 @@ __device__ __forceinline__ void residual_cell(const TopoView& t, const R* __rest
     // 0.0 + x as in apply_cell_flux (it only normalises a -0 result).
     const double r = cell_flux ? acc[k] : std::is_same<R, double>::value ? 0.0 + dtv * acc[k] : dtv * acc[k];
     if (res_out) res_out[k * C + c] = r;
+    // x + a*r: the plain form rounds the product and the sum as the
+    // reference does; the mixed form (FP64 update, no reference bits to keep)
+    // fuses them, an explicit fma that gives the same bits in every build.
+    auto axpy = [&](double x, double a) { return std::is_same<R, double>::value ? x + a * r : fma(a, r, x); };
     if (stage == 0) {
       const double un = Un[k * C + c];
-      Unp1[k * C + c] = un + beta * r;
-      ut[k] = un + alpha_next * r;
+      Unp1[k * C + c] = axpy(un, beta);
+      ut[k] = axpy(un, alpha_next);
     } else if (stage < 3) {
       const double un = Un[k * C + c];
-      Unp1[k * C + c] = Unp1[k * C + c] + beta * r;
-      ut[k] = un + alpha_next * r;
+      Unp1[k * C + c] = axpy(Unp1[k * C + c], beta);
+      ut[k] = axpy(un, alpha_next);
     } else {
-      const double u1 = Unp1[k * C + c] + beta * r;
+      const double u1 = axpy(Unp1[k * C + c], beta);
       Un[k * C + c] = u1;
-      ut[k] = u1 + alpha_next * r;
+      ut[k] = std::is_same<R, double>::value ? u1 + alpha_next * r : u1;  // alpha_next = 0
     }
   }
   store_primitives<R>(ut, W, C, c);

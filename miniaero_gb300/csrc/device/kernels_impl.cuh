@@ -657,7 +657,7 @@ __global__ void __launch_bounds__(kCellBlock) k_residual(TopoView t, const R* __
 // one segment. The chunk count is read from device memory so that a captured
 // graph stays valid when the batch membership changes.
 template <class R, int MODE>
-__global__ void __launch_bounds__(256) kb_sweep1(const Segment<R>* __restrict__ segs, const int2* __restrict__ chunks,
+__global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 0) kb_sweep1(const Segment<R>* __restrict__ segs, const int2* __restrict__ chunks,
                                                  const int* __restrict__ nchunks) {
   const int n = *nchunks;
   for (int ch = blockIdx.x; ch < n; ch += gridDim.x) {

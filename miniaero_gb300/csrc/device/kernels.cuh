@@ -29,7 +29,7 @@ struct TopoView {
   // Per-cell contribution lists, slot-major [kMaxCellFaces][C], code =
   // (face << 1) | (cell is the face's left cell), -1 for an unused slot.
   const int32_t* csr_grad = nullptr;   // Green-Gauss / min-max / limiter order
-  const int32_t* csr_nbr = nullptr;    // neighbour cell of each csr_grad slot (-1 boundary)
+  const int32_t* csr_nbr = nullptr;    // neighbour cell of each csr_grad slot (the cell itself on a boundary face)
   const int32_t* csr_flux = nullptr;   // residual order
   // Bit 0: the cell is axis-aligned and its csr_grad list is grouped by axis
   // (two faces each for x, y, z): gradient terms along other axes are zero.

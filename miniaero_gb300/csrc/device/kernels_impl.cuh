@@ -250,7 +250,11 @@ __device__ __forceinline__ void limiter_cell(const TopoView& t, const GeomView<R
 // face order (GreenGauss.h:79-220), div(a) giving each term a / V; with
 // MINMAX the stencil min/max too. Axis-aligned cells (axis_cell bit 0): slots
 // 2p, 2p+1 are the faces normal to axis p, in serial order, and only the
-// gradient components along p get nonzero terms.
+// gradient components along p get nonzero terms. A boundary face lists the
+// cell as its own neighbour and takes the internal expressions, which give
+// its terms exactly (GreenGauss.h:168-220, min_max_face<false>):
+// 0.5 * (w + w) * n = w * n (w below half the largest finite value), and the
+// min and max of (w, w) are w; so no branch holds back the gathers.
 template <class R, bool MINMAX, class Div>
 __device__ __forceinline__ void green_gauss_cell(const TopoView& t, const GeomView<R>& g, const R* __restrict__ W,
                                                  int c, const R wc[5], R acc[5][3], Extrema<R>* ex, Div div) {
@@ -265,25 +269,17 @@ __device__ __forceinline__ void green_gauss_cell(const TopoView& t, const GeomVi
         const int f = code >> 1;
         const bool left = code & 1;
         const R np = g.fn[p * F + f];
-        if (f < t.Fi) {
-          const int nb = t.csr_nbr[s * C + c];
-          R wn[5];
+        const int nb = t.csr_nbr[s * C + c];
+        R wn[5];
 #pragma unroll
-          for (int k = 0; k < 5; ++k) wn[k] = W[k * C + nb];
+        for (int k = 0; k < 5; ++k) wn[k] = W[k * C + nb];
 #pragma unroll
-          for (int k = 0; k < 5; ++k) {
-            const R pl = left ? wc[k] : wn[k];
-            const R pr = left ? wn[k] : wc[k];
-            const R gr = R(0.5) * (pl + pr) * np;
-            acc[k][p] += div(left ? gr : -gr);
-            if (MINMAX) ex[k].face(pl, pr);
-          }
-        } else {
-#pragma unroll
-          for (int k = 0; k < 5; ++k) {
-            acc[k][p] += div(wc[k] * np);
-            if (MINMAX) ex[k].one(wc[k]);
-          }
+        for (int k = 0; k < 5; ++k) {
+          const R pl = left ? wc[k] : wn[k];
+          const R pr = left ? wn[k] : wc[k];
+          const R gr = R(0.5) * (pl + pr) * np;
+          acc[k][p] += div(left ? gr : -gr);
+          if (MINMAX) ex[k].face(pl, pr);
         }
       }
     }
@@ -296,30 +292,21 @@ __device__ __forceinline__ void green_gauss_cell(const TopoView& t, const GeomVi
     const int f = code >> 1;
     const bool left = code & 1;
     const R n[3] = {g.fn[f], g.fn[F + f], g.fn[2 * F + f]};
-    if (f < t.Fi) {
-      const int nb = t.csr_nbr[s * C + c];
-      R wn[5];
+    const int nb = t.csr_nbr[s * C + c];
+    R wn[5];
 #pragma unroll
-      for (int k = 0; k < 5; ++k) wn[k] = W[k * C + nb];
+    for (int k = 0; k < 5; ++k) wn[k] = W[k * C + nb];
 #pragma unroll
-      for (int k = 0; k < 5; ++k) {
-        const R pl = left ? wc[k] : wn[k];
-        const R pr = left ? wn[k] : wc[k];
-        const R h = R(0.5) * (pl + pr);
+    for (int k = 0; k < 5; ++k) {
+      const R pl = left ? wc[k] : wn[k];
+      const R pr = left ? wn[k] : wc[k];
+      const R h = R(0.5) * (pl + pr);
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          const R gr = h * n[d];
-          acc[k][d] += div(left ? gr : -gr);
-        }
-        if (MINMAX) ex[k].face(pl, pr);
+      for (int d = 0; d < 3; ++d) {
+        const R gr = h * n[d];
+        acc[k][d] += div(left ? gr : -gr);
       }
-    } else {
-#pragma unroll
-      for (int k = 0; k < 5; ++k) {
-#pragma unroll
-        for (int d = 0; d < 3; ++d) acc[k][d] += div(wc[k] * n[d]);
-        if (MINMAX) ex[k].one(wc[k]);
-      }
+      if (MINMAX) ex[k].face(pl, pr);
     }
   }
 }

@@ -314,7 +314,7 @@ extern "C" ma_status ma_mesh_upload_ex(const ma_mesh_view* v, int32_t flags, ma_
     }
     for (int b = 0; b < v->nbc; ++b)  // boundary_faces order
       for (int32_t i = 0; i < v->bc[b].nfaces; ++i)
-        push(csr_grad, ng, v->bc[b].conn[2 * i], ((bc_base[b] + i) << 1) | 1, -1, true);
+        push(csr_grad, ng, v->bc[b].conn[2 * i], ((bc_base[b] + i) << 1) | 1, v->bc[b].conn[2 * i], true);
     for (int r = 0; r < 4; ++r)  // grouped by BC type
       for (int b = 0; b < v->nbc; ++b)
         if (type_rank(v->bc[b].type) == r)
@@ -348,7 +348,7 @@ extern "C" ma_status ma_mesh_upload_ex(const ma_mesh_view* v, int32_t flags, ma_
       }
       for (int b = 0; b < v->nbc && ok; ++b)
         for (int32_t i = 0; i < v->bc[b].nfaces && ok; ++i)
-          ok = put(v->bc[b].conn[2 * i], v->bc[b].flux_index[2 * i], ((bc_base[b] + i) << 1) | 1, -1);
+          ok = put(v->bc[b].conn[2 * i], v->bc[b].flux_index[2 * i], ((bc_base[b] + i) << 1) | 1, v->bc[b].conn[2 * i]);
       if (!ok) return set_error(MA_EINVAL, "flux_index out of range or repeated within a cell");
       cf_flux = cf_grad;  // residual order: plain slot order
     }

@@ -140,9 +140,14 @@ __device__ __forceinline__ void venkat_cell(const TopoView& t, const GeomView<do
                                             const double mn[5], const double mx[5], const double gsum[5][3],
                                             double* __restrict__ phi, int c) {
   const int C = t.C, F = t.F;
-  double nm[5], dm[5];
+  double nm[5], dm[5], dmax[5], dmin[5];
 #pragma unroll
-  for (int k = 0; k < 5; ++k) { nm[k] = 1.0; dm[k] = 1.0; }
+  for (int k = 0; k < 5; ++k) {
+    nm[k] = 1.0;
+    dm[k] = 1.0;
+    dmax[k] = mx[k] - wc[k];  // the stencil differences, once per cell
+    dmin[k] = mn[k] - wc[k];
+  }
   if constexpr (AXIS) {
 #pragma unroll
     for (int p = 0; p < 3; ++p) {
@@ -157,7 +162,7 @@ __device__ __forceinline__ void venkat_cell(const TopoView& t, const GeomView<do
         for (int k = 0; k < 5; ++k) {
           const double du = dp * gsum[k][p];
           double n, dd;
-          if (venkat_ratio(mx[k] - wc[k], mn[k] - wc[k], du, dist, n, dd) && ratio_less(n, dd, nm[k], dm[k])) {
+          if (venkat_ratio(dmax[k], dmin[k], du, dist, n, dd) && ratio_less(n, dd, nm[k], dm[k])) {
             nm[k] = n;
             dm[k] = dd;
           }
@@ -181,7 +186,7 @@ __device__ __forceinline__ void venkat_cell(const TopoView& t, const GeomView<do
 #pragma unroll
         for (int d = 0; d < 3; ++d) du += disp[d] * gsum[k][d];
         double n, dd;
-        if (venkat_ratio(mx[k] - wc[k], mn[k] - wc[k], du, dist, n, dd) && ratio_less(n, dd, nm[k], dm[k])) {
+        if (venkat_ratio(dmax[k], dmin[k], du, dist, n, dd) && ratio_less(n, dd, nm[k], dm[k])) {
           nm[k] = n;
           dm[k] = dd;
         }

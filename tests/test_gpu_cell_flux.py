@@ -74,6 +74,34 @@ def test_mixed_within_tolerance(has_gpu):
     assert np.linalg.norm(U[:, 0] - ref[:, 0]) / np.linalg.norm(ref[:, 0]) < 1e-5
 
 
+def test_cli_gather_cell_flux(has_gpu, tmp_path):
+    """The CLI's `gather cell_flux` line: results.0 of the oracle's CELL_FLUX solve."""
+    from tests.test_gpu_checkpoint import run_cli, write_inp
+    from tests.test_oracle_gold import results_lines
+    case = "flatplate_serial"
+    write_inp(tmp_path / "miniaero.inp", case, steps=40, extra=["gather cell_flux"])
+    run_cli(tmp_path)
+    o = cf(options(case), ntimesteps=40)
+    md = ma.Parallel3DMesh.from_options(o).fill_mesh_data()
+    expected = results_lines(md, oracle.solve(md, o, ma.initial_state(md, o)))
+    assert (tmp_path / "results.0").read_text().splitlines() == expected
+
+
+def test_bad_slots_are_rejected(has_gpu):
+    o = options("sod_serial")
+    md = ma.Parallel3DMesh.from_options(o).fill_mesh_data()
+    # Every hex cell uses all six slots, so moving one face to another slot
+    # makes that slot appear twice within its left cell.
+    md.internal.flux_index[0, 0] = (md.internal.flux_index[0, 0] + 1) % 6
+    with pytest.raises(ma.MiniaeroError, match="flux_index") as e:
+        ma.DeviceMesh(md, cell_flux=True)
+    assert e.value.status == ma._lib.MA_EINVAL
+    md.internal.flux_index = None
+    with pytest.raises(ma.MiniaeroError, match="flux_index"):
+        ma.DeviceMesh(md, cell_flux=True)
+    ma.DeviceMesh(md).close()  # the default lists need no slots
+
+
 def test_mesh_without_slot_lists_is_rejected(has_gpu):
     o = cf(options("sod_serial"))
     md = ma.Parallel3DMesh.from_options(o).fill_mesh_data()

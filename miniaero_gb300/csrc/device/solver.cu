@@ -2,8 +2,9 @@
 //
 // ma_mesh_upload turns a reference-ordered mesh (MeshData, kokkos/MeshData.h)
 // into the device layout:
-//  * internal faces re-ordered by (left, right) cell for locality; face
-//    results do not depend on the order faces are computed in;
+//  * internal faces re-ordered by tile of 4096 left cells, then face class
+//    (axis alignment), then (left, right) cell, for locality and uniform
+//    warps; face results do not depend on the order faces are computed in;
 //  * boundary faces grouped by BC type (Extrapolate, Tangent, NoSlip, Inflow);
 //  * per-face Roe frame |n|, n/|n|, t/|t|, b/|b| and centroid offsets,
 //    computed once with the reference's expressions;

@@ -3,8 +3,8 @@ reference's three serial test cases (kokkos/tests/{3D_Sod,Ramp,FlatPlate}_Serial
 miniaero.inp parameters) computed by the serial oracle, and SHA-256 digests of
 the host mesh arrays (connectivity, permutations, geometry).
 
-The oracle itself is pinned to the reference's results.gold files by
-tests/test_oracle_gold.py; these fixtures carry that pin to machines without
+The oracle itself is pinned to the reference's results.gold and
+results.<rank>.gold files by tests/test_oracle_gold.py; these fixtures carry that pin to machines without
 the reference tree (the GPU tests compare against them bit for bit).
 
 Run from the repository root:  python tests/golden/make_golden.py
@@ -26,6 +26,7 @@ CASES = {
     "sod_serial": (0, 0.3048, 1.0, 1.0, 0.0, 128, 4, 4, 100, 2e-6, 0, 0),
     "ramp_serial": (2, 2.0, 2.0, 1.0, 30.0, 64, 32, 2, 400, 1e-5, 1, 0),
     "flatplate_serial": (1, 2.0, 0.002, 1.0, 0.0, 16, 32, 2, 400, 3e-8, 1, 1),
+    "flatplate_parallel": (1, 2.0, 0.002, 1.0, 0.0, 32, 64, 2, 400, 1e-8, 1, 1),
 }
 
 

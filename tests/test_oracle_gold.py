@@ -1,8 +1,13 @@
 """The oracle (and the host mesh it runs on) against the reference's own
 golden vectors: kokkos/tests/{3D_Sod,Ramp,FlatPlate}_Serial/results.gold,
 compared with the reference's numeric_text_diff rule and tolerances
-(3d_sod_serial_test.sh:4, ramp_serial_test.sh:4, flatplate_serial_test.sh:4).
+(3d_sod_serial_test.sh:4, ramp_serial_test.sh:4, flatplate_serial_test.sh:4),
+and kokkos/tests/{3D_Sod,Ramp,FlatPlate}_Parallel/results.<rank>.gold (4, 16
+and 8 ranks) against one single-rank solve of the same miniaero.inp, cells
+paired by their printed centroid (3d_sod_parallel_test.sh:7,
+ramp_parallel_test.sh:7, flatplate_parallel_test.sh:7).
 Runs where the reference tree is present (CPU container)."""
+import glob
 import os
 
 import numpy as np
@@ -13,6 +18,9 @@ import oracle
 from tests.numeric_text_diff import compare_lines
 
 CASES = [("3D_Sod_Serial", 1e-3, 1e-6), ("Ramp_Serial", 1e-2, 1e-3), ("FlatPlate_Serial", 1e-2, 1e-3)]
+PARALLEL_CASES = [("3D_Sod_Parallel", 4, 1e-3, 1e-6), ("Ramp_Parallel", 16, 1e-2, 1e-3),
+                  ("FlatPlate_Parallel", 8, 1e-2, 1e-3)]
+_solves = {}
 
 
 def results_lines(md, U):
@@ -24,23 +32,58 @@ def results_lines(md, U):
     return lines
 
 
-@pytest.mark.parametrize("case,rel,floor", CASES)
-def test_oracle_matches_reference_gold(reference_dir, case, rel, floor):
-    o = ma.Options.read_options_file(os.path.join(reference_dir, "tests", case, "miniaero.inp"))
-    md = ma.Parallel3DMesh.from_options(o).fill_mesh_data()
-    U = oracle.solve(md, o, ma.initial_state(md, o))
-    with open(os.path.join(reference_dir, "tests", case, "results.gold")) as f:
-        gold = f.read().splitlines()
-    mine = results_lines(md, U)
-    assert compare_lines(mine, gold, rel, floor) == []
-    # Stronger than the reference rule: every field above 1e-3 in magnitude is
-    # textually identical at the 6 printed digits.
+def solve_input(path):
+    """Oracle results lines for a miniaero.inp; cases with equal inputs share one solve."""
+    with open(path) as f:
+        key = f.read().split()
+    key = tuple(key)
+    if key not in _solves:
+        o = ma.Options.read_options_file(path)
+        md = ma.Parallel3DMesh.from_options(o).fill_mesh_data()
+        _solves[key] = results_lines(md, oracle.solve(md, o, ma.initial_state(md, o)))
+    return _solves[key]
+
+
+def textual_mismatches(mine, gold):
+    """Fields above 1e-3 in magnitude that differ at the 6 printed digits."""
     bad = 0
     for a, b in zip(mine, gold):
         for x, y in zip(a.split(), b.split()):
             if x != y and max(abs(float(x)), abs(float(y))) > 1e-3:
                 bad += 1
-    assert bad == 0
+    return bad
+
+
+@pytest.mark.parametrize("case,rel,floor", CASES)
+def test_oracle_matches_reference_gold(reference_dir, case, rel, floor):
+    mine = solve_input(os.path.join(reference_dir, "tests", case, "miniaero.inp"))
+    with open(os.path.join(reference_dir, "tests", case, "results.gold")) as f:
+        gold = f.read().splitlines()
+    assert compare_lines(mine, gold, rel, floor) == []
+    # Stronger than the reference rule: every field above 1e-3 in magnitude is
+    # textually identical at the 6 printed digits.
+    assert textual_mismatches(mine, gold) == 0
+
+
+@pytest.mark.parametrize("case,ranks,rel,floor", PARALLEL_CASES)
+def test_oracle_matches_reference_parallel_gold(reference_dir, case, ranks, rel, floor):
+    """Each rank's results file holds its own cells (centroid, then U); the
+    union over ranks is the whole mesh, each cell once."""
+    d = os.path.join(reference_dir, "tests", case)
+    mine = solve_input(os.path.join(d, "miniaero.inp"))
+    by_centroid = {tuple(line.split()[:3]): line for line in mine}
+    assert len(by_centroid) == len(mine)
+    files = glob.glob(os.path.join(d, "results.*.gold"))
+    assert len(files) == ranks
+    seen = 0
+    for path in sorted(files):
+        with open(path) as f:
+            gold = f.read().splitlines()
+        ours = [by_centroid[tuple(line.split()[:3])] for line in gold]
+        assert compare_lines(ours, gold, rel, floor) == [], path
+        assert textual_mismatches(ours, gold) == 0, path
+        seen += len(gold)
+    assert seen == len(mine)
 
 
 def test_oracle_threads_agree_with_serial():

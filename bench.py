@@ -107,9 +107,24 @@ def stage_roofline(C, prof, w):
             "frac": achieved / peak}
 
 
-def kernel_rooflines(md, prof, w, sm_mhz):
+def fp64_ceiling(kernel, rates):
+    """Measured FP64 ceiling (thread instructions/s) for one kernel's
+    instruction mix: its fused multiply-adds at the measured FMA rate, every
+    other FP64-pipe instruction at the measured add/multiply rate (the lower
+    one on GB300), from the per-item counts of the ncu summary."""
+    n = (load_traffic("fp64_thread_inst_per_item") or {}).get(kernel)
+    f = (load_traffic("fp64_fma_inst_per_item") or {}).get(kernel)
+    if not rates or not n or f is None:
+        return None
+    addmul = 0.5 * (rates["add"] + rates["mul"])
+    return n / (f / rates["fma"] + (n - f) / addmul)
+
+
+def kernel_rooflines(md, prof, w, sm_mhz, fp64_rates=None):
     """Per-kernel time share, achieved algorithmic GB/s and, where the ncu
-    summary gives FP64 instructions per item, FP64-pipe throughput."""
+    summary gives FP64 instructions per item, FP64-pipe throughput against
+    the nominal 2 per SM per clock and against the rates measured on this
+    device (fp64_rates: {"add", "mul", "fma"} thread instructions/s)."""
     total_ms = sum(v[0] for v in prof.values())
     peak, peak_kind = load_peaks()
     fp64 = load_traffic("fp64_thread_inst_per_item") or {}
@@ -126,6 +141,9 @@ def kernel_rooflines(md, prof, w, sm_mhz):
         if w == 8 and k in fp64:
             inst = fp64[k] * items[k]
             e["fp64_pipe_frac"] = inst / (per / 1e3) / fp64_peak
+            ceiling = fp64_ceiling(k, fp64_rates)
+            if ceiling:
+                e["fp64_measured_ceiling_frac"] = inst / (per / 1e3) / ceiling
         kernels[k] = e
     dom = max(kernels, key=lambda k: kernels[k]["share"])
     d = kernels[dom]
@@ -137,6 +155,15 @@ def kernel_rooflines(md, prof, w, sm_mhz):
         roofline["fp64_pipe"] = {"frac": d["fp64_pipe_frac"], "peak_inst_per_s": fp64_peak,
                                  "note": "FP64 thread instructions per item from the ncu summary; the plain form "
                                          "is bound by this pipe, not by HBM"}
+        if fp64_rates:
+            roofline["fp64_pipe"]["measured_rates_inst_per_s"] = fp64_rates
+        ceiling = fp64_ceiling(dom, fp64_rates)
+        if ceiling:
+            roofline["fp64_pipe"].update({
+                "measured_ceiling_inst_per_s": ceiling,
+                "frac_of_measured": d["fp64_measured_ceiling_frac"],
+                "ceiling_note": "add, multiply and fma streams timed on this device by ma_debug_fp64_rate, "
+                                "weighted by the kernel's FMA share of FP64 instructions"})
     return roofline, kernels
 
 
@@ -384,7 +411,8 @@ def run_ours(args, world, rank, local):
     # ---- per-kernel durations (same workload, kernels launched one by one) ----
     prof = solver.profile_steps(max(2, min(args.steps, 10)))
     Fi = md.internal.nfaces
-    roofline, kernels = kernel_rooflines(md, prof, 8, clocks.get("sm_mhz"))
+    fp64_rates = {op: ma.fp64_rate(op) for op in ("add", "mul", "fma")}
+    roofline, kernels = kernel_rooflines(md, prof, 8, clocks.get("sm_mhz"), fp64_rates)
     roofline["stage"] = stage_roofline(C, prof, 8)
 
     # ---- mixed form on the same mesh: throughput and error vs FP64 ----

@@ -356,6 +356,13 @@ ma_status ma_debug_binsort(const int32_t* keys, int32_t n, int32_t* perm);
  * example[0..1]. */
 ma_status ma_debug_check_division(int32_t mode, uint64_t n, uint64_t seed, uint64_t* mismatches, double* example);
 
+/* Measured FP64 issue rate of this device (thread instructions per second):
+ * op 0 additions, 1 multiplications, 2 fused multiply-adds, each as 4
+ * independent chains per thread on 8 blocks of 256 threads per SM; the best
+ * of 3 timed launches after one warm-up. The ceiling the FP64 form's kernels
+ * are measured against. */
+ma_status ma_debug_fp64_rate(int32_t op, double* inst_per_s);
+
 /* ---- operator-level entry points (unit parity; host arrays in and out) --- */
 /* roe_flux::compute_flux (Roe_Flux.h:50) on n independent faces:
  * pl, pr [n*5] primitives; normal, tangent, binormal [n*3]; flux [n*5]. */

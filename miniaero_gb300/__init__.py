@@ -593,3 +593,12 @@ def compute_primitives(U):
     out = np.empty_like(U)
     check(lib().ma_op_primitives(U.shape[0], f64p(U), f64p(out)))
     return out
+
+
+def fp64_rate(op):
+    """Measured FP64 thread-instruction rate of the current device for
+    additions ("add"), multiplications ("mul") or fused multiply-adds ("fma")."""
+    code = {"add": 0, "mul": 1, "fma": 2}[op]
+    r = ctypes.c_double()
+    check(lib().ma_debug_fp64_rate(code, ctypes.byref(r)))
+    return r.value

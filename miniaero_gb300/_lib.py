@@ -219,6 +219,7 @@ _SIGNATURES = {
     "ma_debug_binsort": (c_int32, [P_i32, c_int32, P_i32]),
     "ma_debug_check_division": (c_int32, [c_int32, ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64),
                                           P_f64]),
+    "ma_debug_fp64_rate": (c_int32, [c_int32, P_f64]),
     "ma_op_roe_flux": (c_int32, [c_int32, P_f64, P_f64, P_f64, P_f64, P_f64, P_f64]),
     "ma_op_viscous_flux": (c_int32, [c_int32, P_f64, P_f64, P_f64, c_int32, c_double, c_double, P_f64]),
     "ma_op_limiter": (c_int32, [c_int32, c_int32, P_f64, P_f64, P_f64, P_f64, P_f64]),

@@ -162,6 +162,10 @@ cudaError_t launch_op_primitives(int n, const double* U, double* V, cudaStream_t
 cudaError_t launch_check_division(int mode, unsigned long long n, unsigned long long seed,
                                   unsigned long long* mismatches, double* example, cudaStream_t stream);
 
+// FP64 issue-rate kernel: blocks x 256 threads, 4 chains of iters operations
+// each (op 0 add, 1 multiply, 2 fused multiply-add); out holds one double per thread.
+cudaError_t launch_fp64_rate(int op, int blocks, int iters, double* out, cudaStream_t stream);
+
 // State check: first cell with a non-finite value or non-positive rho / rhoE.
 cudaError_t launch_check_state(int C, const double* Un, unsigned long long* first_bad, cudaStream_t stream);
 

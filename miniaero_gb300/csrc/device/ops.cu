@@ -155,6 +155,22 @@ __global__ void k_check_division(int mode, unsigned long long n, unsigned long l
   }
 }
 
+// FP64 issue rate: 4 independent chains of one operation per thread
+// (op 0 x + y, 1 x * y, 2 fma(x, y, y)); y comes in as a parameter so the
+// chains cannot be folded, and each thread stores its sum.
+template <int OP>
+__global__ void __launch_bounds__(256) k_fp64_rate(int iters, double y, double* __restrict__ out) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  double x[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) x[j] = 1.0 + 1e-3 * (tid + j);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) x[j] = OP == 0 ? x[j] + y : OP == 1 ? x[j] * y : fma(x[j], y, y);
+  }
+  out[tid] = (x[0] + x[1]) + (x[2] + x[3]);
+}
+
 // dt = cfl * min_c V_c / sum_f (|u.n| + c |n|) on the current U_n.
 __global__ void k_cfl(TopoView t, GeomView<double> g, const double* __restrict__ Un,
                       unsigned long long* out) {
@@ -219,6 +235,14 @@ cudaError_t launch_op_primitives(int n, const double* U, double* V, cudaStream_t
 cudaError_t launch_check_division(int mode, unsigned long long n, unsigned long long seed,
                                   unsigned long long* mismatches, double* example, cudaStream_t stream) {
   k_check_division<<<152 * 8, 256, 0, stream>>>(mode, n, seed, mismatches, example);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fp64_rate(int op, int blocks, int iters, double* out, cudaStream_t stream) {
+  const double y = op == 1 ? 1.0000001 : 1e-9;
+  if (op == 0) k_fp64_rate<0><<<blocks, 256, 0, stream>>>(iters, y, out);
+  else if (op == 1) k_fp64_rate<1><<<blocks, 256, 0, stream>>>(iters, y, out);
+  else k_fp64_rate<2><<<blocks, 256, 0, stream>>>(iters, y, out);
   return cudaGetLastError();
 }
 

@@ -934,6 +934,36 @@ extern "C" ma_status ma_debug_check_division(int32_t mode, uint64_t n, uint64_t 
   return MA_OK;
 }
 
+extern "C" ma_status ma_debug_fp64_rate(int32_t op, double* inst_per_s) {
+  if (!inst_per_s || op < 0 || op > 2) return set_error(MA_EINVAL, "ma_debug_fp64_rate: bad arguments");
+  int dev = 0, sms = 0;
+  MA_CUDA_TRY(cudaGetDevice(&dev));
+  MA_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int blocks = 8 * sms, iters = 2048;
+  DevBufs b;
+  double* out;
+  MA_CUDA_TRY(b.in(nullptr, static_cast<size_t>(blocks) * 256, &out));
+  cudaEvent_t e0, e1;
+  MA_CUDA_TRY(cudaEventCreate(&e0));
+  cudaError_t err = cudaEventCreate(&e1);
+  float best = 0.f;
+  for (int r = 0; r < 4 && err == cudaSuccess; ++r) {
+    err = cudaEventRecord(e0, 0);
+    if (err == cudaSuccess) err = dev::launch_fp64_rate(op, blocks, iters, out, 0);
+    if (err == cudaSuccess) err = cudaEventRecord(e1, 0);
+    if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+    if (r > 0 && (best == 0.f || ms < best)) best = ms;  // launch 0 warms up
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  MA_CUDA_TRY(err);
+  if (!(best > 0.f)) return set_error(MA_ENUMERIC, "ma_debug_fp64_rate: no elapsed time");
+  *inst_per_s = static_cast<double>(blocks) * 256.0 * iters * 4.0 / (best * 1e-3);
+  return MA_OK;
+}
+
 extern "C" ma_status ma_op_primitives(int32_t n, const double* U, double* V) {
   if (n < 0 || (n > 0 && (!U || !V))) return set_error(MA_EINVAL, "ma_op_primitives: bad arguments");
   if (n == 0) return MA_OK;

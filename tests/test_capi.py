@@ -95,6 +95,8 @@ def test_device_calls_fail_cleanly_without_gpu():
     assert e.value.status == _lib.MA_ECUDA
     with pytest.raises(ma.MiniaeroError):
         ma.roe_flux([[1, 0, 0, 0, 300]], [[1, 0, 0, 0, 300]], [[1, 0, 0]], [[0, 1, 0]], [[0, 0, 1]])
+    with pytest.raises(ma.MiniaeroError):
+        ma.fp64_rate("add")
 
 
 def test_upload_rejects_bad_meshes():

@@ -249,3 +249,15 @@ def test_reciprocal_division_is_correctly_rounded(has_gpu, mode):
     ex = np.zeros(2)
     _lib.check(_lib.lib().ma_debug_check_division(mode, 1 << 28, 12345 + mode, ctypes.byref(mism), _lib.f64p(ex)))
     assert mism.value == 0, "first mismatch a=%r b=%r" % (ex[0], ex[1])
+
+
+def test_fp64_rate_is_measured(has_gpu):
+    """The FP64 ceiling the bench reports against: three positive, finite
+    rates of at least one instruction per SM per 100 clocks."""
+    for op in ("add", "mul", "fma"):
+        r = ma.fp64_rate(op)
+        assert np.isfinite(r) and r > 152 * 1e9 / 100, (op, r)
+    import ctypes
+    from miniaero_gb300 import _lib
+    with pytest.raises(ma.MiniaeroError):
+        _lib.check(_lib.lib().ma_debug_fp64_rate(3, ctypes.byref(ctypes.c_double())))

@@ -278,6 +278,11 @@ ma_status ma_batch_set_launch(ma_batch* b, const int32_t* block, const int32_t* 
  * restored afterwards. best_ms (4 values, may be NULL) receives the chosen
  * per-launch times. */
 ma_status ma_batch_autotune(ma_batch* b, int32_t reps, double* best_ms);
+/* Advances every member nsteps steps like ma_batch_step, but launching the
+ * kernels one by one (no graph) with CUDA events around each on the batch's
+ * stream; returns summed milliseconds and launch counts per kernel kind
+ * (arrays of MA_PROFILE_KINDS). */
+ma_status ma_batch_profile_steps(ma_batch* b, int32_t nsteps, double* kernel_ms, int32_t* kernel_launches);
 
 /* ---- serving loop -------------------------------------------------------
  * No reference counterpart: the reference runs one solve per invocation

@@ -421,6 +421,13 @@ class Batch:
         check(lib().ma_batch_autotune(self._h, int(reps), f64p(best)))
         return best
 
+    def profile_steps(self, nsteps):
+        """Steps with CUDA events around each kernel; {kind: (ms_total, launches)}."""
+        ms = np.zeros(_lib.MA_PROFILE_KINDS, np.float64)
+        n = np.zeros(_lib.MA_PROFILE_KINDS, np.int32)
+        check(lib().ma_batch_profile_steps(self._h, int(nsteps), f64p(ms), i32p(n)))
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(_lib.KERNEL_KINDS) if n[i] > 0}
+
     @property
     def launch(self):
         b = np.zeros(4, np.int32)

@@ -365,6 +365,61 @@ extern "C" ma_status ma_batch_step(ma_batch* b, int32_t nsteps) {
   return MA_OK;
 }
 
+extern "C" ma_status ma_batch_profile_steps(ma_batch* b, int32_t nsteps, double* kernel_ms, int32_t* kernel_launches) {
+  if (!b || nsteps < 0 || !kernel_ms || !kernel_launches)
+    return set_error(MA_EINVAL, "ma_batch_profile_steps: bad arguments");
+  for (int k = 0; k < MA_PROFILE_KINDS; ++k) {
+    kernel_ms[k] = 0.0;
+    kernel_launches[k] = 0;
+  }
+  if (nsteps == 0 || b->members.empty()) return MA_OK;
+  if (b->tables_dirty) {
+    ma_status st = upload_tables(b);
+    if (st != MA_OK) return st;
+  }
+  const unsigned bits[MA_PROFILE_KINDS] = {dev::kSweep1, dev::kInternalFlux, dev::kBcFlux, dev::kResidual};
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> kind;
+  auto cleanup = [&]() { for (cudaEvent_t e : ev) cudaEventDestroy(e); };
+  for (int32_t step = 0; step < nsteps; ++step)
+    for (int stage = 0; stage < 4; ++stage)
+      for (int k = 0; k < MA_PROFILE_KINDS; ++k) {
+        cudaEvent_t a, e;
+        if (cudaEventCreate(&a) != cudaSuccess) {
+          cleanup();
+          return set_error(MA_ECUDA, "ma_batch_profile_steps: cudaEventCreate failed");
+        }
+        ev.push_back(a);
+        if (cudaEventCreate(&e) != cudaSuccess) {
+          cleanup();
+          return set_error(MA_ECUDA, "ma_batch_profile_steps: cudaEventCreate failed");
+        }
+        ev.push_back(e);
+        kind.push_back(k);
+        cudaEventRecord(a, b->stream);
+        ma_status st = launch_stage(b, stage, bits[k]);
+        cudaEventRecord(e, b->stream);
+        if (st != MA_OK) {
+          cleanup();
+          return st;
+        }
+      }
+  cudaError_t err = cudaStreamSynchronize(b->stream);
+  if (err != cudaSuccess) {
+    cleanup();
+    return set_error(MA_ECUDA, std::string("ma_batch_profile_steps: ") + cudaGetErrorString(err));
+  }
+  for (size_t i = 0; i < kind.size(); ++i) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev[2 * i], ev[2 * i + 1]);
+    kernel_ms[kind[i]] += ms;
+    kernel_launches[kind[i]] += 1;
+  }
+  cleanup();
+  for (auto& kv : b->members) kv.second.steps += nsteps;
+  return MA_OK;
+}
+
 extern "C" ma_status ma_batch_synchronize(ma_batch* b) {
   if (!b) return set_error(MA_EINVAL, "ma_batch_synchronize: null batch");
   MB_CUDA_TRY(cudaStreamSynchronize(b->stream));

@@ -475,22 +475,18 @@ __device__ __forceinline__ void viscous_flux_axis(const R g[5][3], const R prim[
   vflux[4] = v4;
 }
 
+// The reference's two branches (du > 1e-40 with dumax, du < -1e-40 with
+// dumin) are one expression with the stencil difference selected first, so a
+// warp whose cells see both signs evaluates it once.
 template <class R>
 __device__ __forceinline__ R venkat(R dumax, R dumin, R du, R deltax3) {
   const R eps2 = deltax3;  // deltax3 * beta^3 with beta = 1
-  R phi;
-  if (du > R(1e-40)) {
-    const R num = (dumax * dumax + eps2) * du + R(2) * du * du * dumax;
-    const R den = du * (dumax * dumax + R(2) * du * du + dumax * du + eps2);
-    phi = num / den;
-  } else if (du < R(-1e-40)) {
-    const R num = (dumin * dumin + eps2) * du + R(2) * du * du * dumin;
-    const R den = du * (dumin * dumin + R(2) * du * du + dumin * du + eps2);
-    phi = num / den;
-  } else {
-    phi = R(1);
-  }
-  return phi;
+  const bool pos = du > R(1e-40), neg = du < R(-1e-40);
+  if (!(pos || neg)) return R(1);
+  const R dm = pos ? dumax : dumin;
+  const R num = (dm * dm + eps2) * du + R(2) * du * du * dm;
+  const R den = du * (dm * dm + R(2) * du * du + dm * du + eps2);
+  return num / den;
 }
 
 // Numerator and denominator of the Venkatakrishnan function, rounded exactly
@@ -514,19 +510,15 @@ __device__ __forceinline__ long long okey(double x) { return ckey(ikey(x)); }
 
 __device__ __forceinline__ bool venkat_ratio(double dumax, double dumin, double du, double eps2, double& n,
                                              double& d) {
-  // du > 1e-40 and du < -1e-40 as key comparisons (same result for non-NaN du).
+  // du > 1e-40 and du < -1e-40 as key comparisons (same result for non-NaN
+  // du); one evaluation with the selected difference, as in venkat().
   const long long kd = okey(du);
-  if (kd > okey(1e-40)) {
-    n = (dumax * dumax + eps2) * du + 2 * du * du * dumax;
-    d = du * (dumax * dumax + 2 * du * du + dumax * du + eps2);
-    return true;
-  }
-  if (kd < okey(-1e-40)) {
-    n = -((dumin * dumin + eps2) * du + 2 * du * du * dumin);
-    d = -(du * (dumin * dumin + 2 * du * du + dumin * du + eps2));
-    return true;
-  }
-  return false;
+  const bool pos = kd > okey(1e-40), neg = kd < okey(-1e-40);
+  if (!(pos | neg)) return false;
+  const double dm = pos ? dumax : dumin;
+  n = negate_if((dm * dm + eps2) * du + 2 * du * du * dm, neg);
+  d = negate_if(du * (dm * dm + 2 * du * du + dm * du + eps2), neg);
+  return true;
 }
 
 // Exact test n1/d1 < n2/d2 for d1, d2 > 0: compares n1*d2 with n2*d1 as
@@ -541,10 +533,12 @@ __device__ __forceinline__ bool ratio_less(double n1, double d1, double n2, doub
 
 template <class R>
 __device__ __forceinline__ R vanalbada(R dumax, R dumin, R du) {
-  // The reference's threshold is DBL_EPSILON in both precisions.
+  // The reference's threshold is DBL_EPSILON in both precisions. Its two
+  // quotients (dumax / du for du > eps, dumin / du for du < -eps) are one
+  // division of the selected difference.
+  const bool pos = du > R(DBL_EPSILON), neg = du < R(-DBL_EPSILON);
   R y = R(2);
-  if (du > R(DBL_EPSILON)) y = dumax / du;
-  else if (du < R(-DBL_EPSILON)) y = dumin / du;
+  if (pos || neg) y = (pos ? dumax : dumin) / du;
   R phi = R(1);
   if (y < R(2)) {
     phi = (R(4) * y - y * y) / (y * y - R(4) * y + R(8));

@@ -112,3 +112,27 @@ def test_batch_budget_is_enforced(has_gpu):
     assert e.value.status == 4  # MA_EBUDGET
     assert b.size == 2 and b.device_bytes == 2 * need
     b.close()
+
+
+def test_batch_profile_steps_equal_graph_steps(has_gpu):
+    """Kernel-by-kernel profiled steps advance members to the same bits as
+    the graph-launched step, and count one launch per kind per stage."""
+    o = sod_options()
+    cases = [member(o, d, 4.0, 6.0) for d in [(10, 6, 4), (6, 5, 7)]]
+    out = []
+    for profiled in (False, True):
+        b = ma.Batch(o, capacity=4, budget_bytes=1 << 30)
+        ids = [b.add(ma.DeviceMesh(md), U0) for (m, md, U0) in cases]
+        if profiled:
+            prof = b.profile_steps(3)
+            assert set(prof) == {"sweep_gradient_limiter", "internal_face_flux", "boundary_face_flux",
+                                 "residual_rk_update"}
+            assert all(n == 12 and ms > 0.0 for ms, n in prof.values())
+        else:
+            b.step(3)
+        b.synchronize()
+        assert all(b.member_steps(i) == 3 for i in ids)
+        out.append([b.get_state(i) for i in ids])
+        b.close()
+    for a, c in zip(*out):
+        assert np.array_equal(a, c)

@@ -584,28 +584,36 @@ __device__ __forceinline__ void residual_cell(const TopoView& t, const R* __rest
     case 2: beta = 1.0 / 3.0; alpha_next = 1.0; break;
     default: beta = 1.0 / 6.0; alpha_next = 0.0; break;
   }
+  // The mixed form's ATOMICS_FLUX update takes the flux sum itself with the
+  // coefficients beta dt/V and alpha dt/V (one multiply each instead of dt/V
+  // times each of the 5 sums); the plain form keeps the reference's
+  // res = 0 + (dt/V) sum and U + beta res.
+  constexpr bool kPlain = std::is_same<R, double>::value;
+  const bool fold = !kPlain && !cell_flux;
+  const double cb = fold ? beta * dtv : beta;
+  const double ca = fold ? alpha_next * dtv : alpha_next;
   double ut[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
     // 0.0 + x as in apply_cell_flux (it only normalises a -0 result).
-    const double r = cell_flux ? acc[k] : std::is_same<R, double>::value ? 0.0 + dtv * acc[k] : dtv * acc[k];
-    if (res_out) res_out[k * C + c] = r;
+    const double r = cell_flux ? acc[k] : kPlain ? 0.0 + dtv * acc[k] : acc[k];
+    if (res_out) res_out[k * C + c] = fold ? dtv * acc[k] : r;
     // x + a*r: the plain form rounds the product and the sum as the
     // reference does; the mixed form (FP64 update, no reference bits to keep)
     // fuses them, an explicit fma that gives the same bits in every build.
-    auto axpy = [&](double x, double a) { return std::is_same<R, double>::value ? x + a * r : fma(a, r, x); };
+    auto axpy = [&](double x, double a) { return kPlain ? x + a * r : fma(a, r, x); };
     if (stage == 0) {
       const double un = Un[k * C + c];
-      Unp1[k * C + c] = axpy(un, beta);
-      ut[k] = axpy(un, alpha_next);
+      Unp1[k * C + c] = axpy(un, cb);
+      ut[k] = axpy(un, ca);
     } else if (stage < 3) {
       const double un = Un[k * C + c];
-      Unp1[k * C + c] = axpy(Unp1[k * C + c], beta);
-      ut[k] = axpy(un, alpha_next);
+      Unp1[k * C + c] = axpy(Unp1[k * C + c], cb);
+      ut[k] = axpy(un, ca);
     } else {
-      const double u1 = axpy(Unp1[k * C + c], beta);
+      const double u1 = axpy(Unp1[k * C + c], cb);
       Un[k * C + c] = u1;
-      ut[k] = std::is_same<R, double>::value ? u1 + alpha_next * r : u1;  // alpha_next = 0
+      ut[k] = kPlain ? u1 + alpha_next * r : u1;  // alpha_next = 0
     }
   }
   store_primitives<R>(ut, W, C, c);

@@ -68,6 +68,8 @@ struct ma_batch {
   size_t used = 0;
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;  // graph side branch: the boundary-face flux
+  cudaEvent_t fork = nullptr, join = nullptr;
   std::map<int32_t, Member> members;
   int32_t next_id = 0;
   // device tables
@@ -158,22 +160,41 @@ ma_status upload_tables(ma_batch* b) {
   return MA_OK;
 }
 
-ma_status launch_stage(ma_batch* b, int stage, unsigned kernels) {
+ma_status launch_stage_on(ma_batch* b, int stage, unsigned kernels, cudaStream_t stream) {
   cudaError_t e = b->mixed
       ? dev::launch_batch_stage<float>(b->cfg, static_cast<const dev::Segment<float>*>(b->d_segs), b->launch, stage,
-                                       b->stream, kernels)
+                                       stream, kernels)
       : dev::launch_batch_stage<double>(b->cfg, static_cast<const dev::Segment<double>*>(b->d_segs), b->launch, stage,
-                                        b->stream, kernels);
+                                        stream, kernels);
   if (e != cudaSuccess) return set_error(MA_ECUDA, std::string("batch stage launch: ") + cudaGetErrorString(e));
   return MA_OK;
 }
+
+ma_status launch_stage(ma_batch* b, int stage, unsigned kernels) { return launch_stage_on(b, stage, kernels, b->stream); }
 
 ma_status capture_graph(ma_batch* b) {
   drop_graph(b);
   cudaGraph_t g = nullptr;
   MB_CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   ma_status st = MA_OK;
-  for (int stage = 0; stage < 4 && st == MA_OK; ++stage) st = launch_stage(b, stage, dev::kAllKernels);
+  // Per stage, the boundary-face flux (it reads only the stage's primitives)
+  // runs on a side branch beside the sweep and the internal-face flux; the
+  // residual waits for both branches.
+  for (int stage = 0; stage < 4 && st == MA_OK; ++stage) {
+    cudaError_t ef = cudaEventRecord(b->fork, b->stream);
+    if (ef == cudaSuccess) ef = cudaStreamWaitEvent(b->side, b->fork, 0);
+    if (ef != cudaSuccess) {
+      st = set_error(MA_ECUDA, std::string("batch capture: ") + cudaGetErrorString(ef));
+      break;
+    }
+    st = launch_stage_on(b, stage, dev::kBcFlux, b->side);
+    if (st == MA_OK && cudaEventRecord(b->join, b->side) != cudaSuccess)
+      st = set_error(MA_ECUDA, "batch capture: join record failed");
+    if (st == MA_OK) st = launch_stage(b, stage, dev::kSweep1 | dev::kInternalFlux);
+    if (st == MA_OK && cudaStreamWaitEvent(b->stream, b->join, 0) != cudaSuccess)
+      st = set_error(MA_ECUDA, "batch capture: join wait failed");
+    if (st == MA_OK) st = launch_stage(b, stage, dev::kResidual);
+  }
   cudaError_t e = cudaStreamEndCapture(b->stream, &g);
   if (st != MA_OK || e != cudaSuccess) {
     if (g) cudaGraphDestroy(g);
@@ -216,6 +237,9 @@ extern "C" ma_status ma_batch_create(const ma_options* o, int32_t capacity, size
   MB_CUDA_TRY(cudaMemset(b->d_nchunks, 0, 4 * sizeof(int) + 8));
   b->d_scratch = reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(b->d_nchunks) + 16);
   MB_CUDA_TRY(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  MB_CUDA_TRY(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
+  MB_CUDA_TRY(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+  MB_CUDA_TRY(cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming));
   for (int k = 0; k < 4; ++k) b->launch.block[k] = 128;
   default_grid(b.get());
   *out = b.release();
@@ -230,6 +254,9 @@ extern "C" void ma_batch_free(ma_batch* b) {
   for (int k = 0; k < 4; ++k) cudaFree(b->d_chunks[k]);
   cudaFree(b->d_segs);
   cudaFree(b->d_nchunks);
+  if (b->join) cudaEventDestroy(b->join);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->side) cudaStreamDestroy(b->side);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
 }

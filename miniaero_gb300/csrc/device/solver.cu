@@ -70,6 +70,8 @@ struct ma_solver {
   dev::PathConfig cfg;
   bool mixed = false;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;       // graph side branch: the boundary-face flux
+  cudaEvent_t fork = nullptr, join = nullptr;
   dev::StateBuffers st;
   dev::StageBuffers<double> b64;
   dev::StageBuffers<float> b32;
@@ -549,10 +551,24 @@ ma_status capture_step_graph(ma_solver* s) {
   MA_CUDA_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   cudaError_t e = cudaSuccess;
   for (int stage = 0; stage < 4 && e == cudaSuccess; ++stage) {
-    if (s->mixed)
-      e = dev::launch_stage<float>(s->topo, s->mesh->g32, s->cfg, s->st, s->b32, stage, s->stream);
-    else
-      e = dev::launch_stage<double>(s->topo, s->mesh->g64, s->cfg, s->st, s->b64, stage, s->stream);
+    auto launch = [&](cudaStream_t stream, unsigned kernels) {
+      return s->mixed
+                 ? dev::launch_stage<float>(s->topo, s->mesh->g32, s->cfg, s->st, s->b32, stage, stream, kernels)
+                 : dev::launch_stage<double>(s->topo, s->mesh->g64, s->cfg, s->st, s->b64, stage, stream, kernels);
+    };
+    // The boundary-face flux reads only the stage's primitives and writes its
+    // own flux slots: a side branch of the graph runs it beside the sweep and
+    // the internal-face flux, and the residual waits for both branches.
+    const bool fork = s->topo.Fb > 0;
+    if (fork) {
+      e = cudaEventRecord(s->fork, s->stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s->side, s->fork, 0);
+      if (e == cudaSuccess) e = launch(s->side, dev::kBcFlux);
+      if (e == cudaSuccess) e = cudaEventRecord(s->join, s->side);
+    }
+    if (e == cudaSuccess) e = launch(s->stream, dev::kSweep1 | dev::kInternalFlux);
+    if (e == cudaSuccess && fork) e = cudaStreamWaitEvent(s->stream, s->join, 0);
+    if (e == cudaSuccess) e = launch(s->stream, dev::kResidual);
   }
   cudaError_t e2 = cudaStreamEndCapture(s->stream, &g);
   if (e != cudaSuccess || e2 != cudaSuccess) {
@@ -628,10 +644,13 @@ extern "C" ma_status ma_solver_create(ma_mesh* mesh, const ma_options* o, ma_sol
   s->bytes = bytes;
   e = cudaMemset(s->dmem, 0, bytes);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming);
   if (e != cudaSuccess) {
-    cudaFree(s->dmem);
-    delete s;
-    return set_error(MA_ECUDA, std::string("ma_solver_create: ") + cudaGetErrorString(e));
+    const std::string msg = std::string("ma_solver_create: ") + cudaGetErrorString(e);
+    ma_solver_free(s);
+    return set_error(MA_ECUDA, msg);
   }
   *out = s;
   return MA_OK;
@@ -641,6 +660,9 @@ extern "C" void ma_solver_free(ma_solver* s) {
   if (!s) return;
   if (s->stream) cudaStreamSynchronize(s->stream);
   if (s->graph) cudaGraphExecDestroy(s->graph);
+  if (s->join) cudaEventDestroy(s->join);
+  if (s->fork) cudaEventDestroy(s->fork);
+  if (s->side) cudaStreamDestroy(s->side);
   if (s->stream) cudaStreamDestroy(s->stream);
   cudaFree(s->dmem);
   delete s;

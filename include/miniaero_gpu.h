@@ -384,6 +384,28 @@ ma_status ma_op_limiter(int32_t n, int32_t kind, const double* dumax, const doub
 /* ComputePrimitives (GasModel.h:69), U and V [n*5]. */
 ma_status ma_op_primitives(int32_t n, const double* U, double* V);
 
+/* One RK stage's drivers taken one at a time on an uploaded mesh and a
+ * conserved state U (ncells x 5 in `layout`), in the reference's serial
+ * (ATOMICS_FLUX) order; outputs are cell-major like the reference's host
+ * views. The solver runs the same kernels fused into its four per stage. */
+/* GreenGauss::compute_gradients (GreenGauss.h:300-321): gradients of the
+ * primitives, grad [ncells*15] as (cell, component, direction). */
+ma_status ma_op_green_gauss(ma_mesh* mesh, const double* U, int32_t layout, double* grad);
+/* StencilLimiter::compute_min_max + compute_limiter (StencilLimiter.h:532-616)
+ * with the Green-Gauss gradient of the same U and limiter MA_LIMITER_*:
+ * phi [ncells*5]. */
+ma_status ma_op_stencil_limiter(ma_mesh* mesh, int32_t limiter, const double* U, int32_t layout, double* phi);
+/* The boundary functors compute_{extrapolate,tangent,NoSlip,inflow}BC_flux as
+ * Solve applies them (TimeSolverExplicitRK4.h:428-475): each cell's boundary
+ * contributions to cell_flux, summed from zero, [ncells*5]. o supplies the
+ * viscosity model (NoSlip is always viscous) and the inflow state. */
+ma_status ma_op_bc_flux(ma_mesh* mesh, const ma_options* o, const double* U, int32_t layout, double* cell_flux);
+/* apply_cell_flux (Flux.h:188-229): res = 0 + (dt / V) * cell_flux, [ncells*5]. */
+ma_status ma_op_apply_cell_flux(int32_t ncells, double dt, const double* volumes, const double* cell_flux,
+                                double* res);
+/* update (TimeSolverExplicitRK4.h:106-128): dst = src + alpha * res over n values. */
+ma_status ma_op_rk_update(int64_t n, double alpha, const double* res, const double* src, double* dst);
+
 #ifdef __cplusplus
 }
 #endif

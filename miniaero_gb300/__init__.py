@@ -609,3 +609,49 @@ def fp64_rate(op):
     r = ctypes.c_double()
     check(lib().ma_debug_fp64_rate(code, ctypes.byref(r)))
     return r.value
+
+
+# ---- one RK stage's drivers on a DeviceMesh and a state (n cells x 5) ----
+def green_gauss(mesh, U):
+    """GreenGauss::compute_gradients: gradients of the primitives of U, (ncells, 5, 3)."""
+    U = _a(U, (mesh.ncells, 5))
+    out = np.empty((mesh.ncells, 5, 3), np.float64)
+    check(lib().ma_op_green_gauss(mesh._h, f64p(U), MA_LAYOUT_AOS, f64p(out)))
+    return out
+
+
+def stencil_limiter(mesh, U, limiter=MA_LIMITER_VENKAT):
+    """StencilLimiter::compute_min_max + compute_limiter with U's Green-Gauss
+    gradient: (ncells, 5)."""
+    U = _a(U, (mesh.ncells, 5))
+    out = np.empty((mesh.ncells, 5), np.float64)
+    check(lib().ma_op_stencil_limiter(mesh._h, int(limiter), f64p(U), MA_LAYOUT_AOS, f64p(out)))
+    return out
+
+
+def bc_flux(mesh, options, U):
+    """The boundary functors as Solve applies them: each cell's boundary
+    contributions to cell_flux, (ncells, 5); options supply the viscosity
+    model and the inflow state."""
+    U = _a(U, (mesh.ncells, 5))
+    out = np.empty((mesh.ncells, 5), np.float64)
+    check(lib().ma_op_bc_flux(mesh._h, ctypes.byref(options._o), f64p(U), MA_LAYOUT_AOS, f64p(out)))
+    return out
+
+
+def apply_cell_flux(dt, volumes, cell_flux):
+    """apply_cell_flux: res = 0 + (dt / V) * cell_flux, (ncells, 5)."""
+    v = _a(volumes, (-1,))
+    f = _a(cell_flux, (v.shape[0], 5))
+    out = np.empty_like(f)
+    check(lib().ma_op_apply_cell_flux(v.shape[0], float(dt), f64p(v), f64p(f), f64p(out)))
+    return out
+
+
+def rk_update(alpha, res, src):
+    """update: src + alpha * res, elementwise."""
+    src = np.ascontiguousarray(src, dtype=np.float64)
+    res = _a(res, src.shape)
+    out = np.empty_like(src)
+    check(lib().ma_op_rk_update(src.size, float(alpha), f64p(res), f64p(src), f64p(out)))
+    return out

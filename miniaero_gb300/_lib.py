@@ -225,6 +225,11 @@ _SIGNATURES = {
     "ma_op_viscous_flux": (c_int32, [c_int32, P_f64, P_f64, P_f64, c_int32, c_double, c_double, P_f64]),
     "ma_op_limiter": (c_int32, [c_int32, c_int32, P_f64, P_f64, P_f64, P_f64, P_f64]),
     "ma_op_primitives": (c_int32, [c_int32, P_f64, P_f64]),
+    "ma_op_green_gauss": (c_int32, [c_void_p, P_f64, c_int32, P_f64]),
+    "ma_op_stencil_limiter": (c_int32, [c_void_p, c_int32, P_f64, c_int32, P_f64]),
+    "ma_op_bc_flux": (c_int32, [c_void_p, ctypes.POINTER(ma_options), P_f64, c_int32, P_f64]),
+    "ma_op_apply_cell_flux": (c_int32, [c_int32, c_double, P_f64, P_f64, P_f64]),
+    "ma_op_rk_update": (c_int32, [ctypes.c_int64, c_double, P_f64, P_f64, P_f64]),
 }
 
 

@@ -162,6 +162,17 @@ cudaError_t launch_op_primitives(int n, const double* U, double* V, cudaStream_t
 cudaError_t launch_check_division(int mode, unsigned long long n, unsigned long long seed,
                                   unsigned long long* mismatches, double* example, cudaStream_t stream);
 
+// Each cell's boundary-face contributions (fflux slots Fi..F-1) summed in the
+// cell's residual list order from +0: out [5][C].
+cudaError_t launch_bc_gather(const TopoView& t, const double* fflux, double* out, cudaStream_t stream);
+// W = ComputePrimitives(U) on [5][C] arrays, U taken as given.
+cudaError_t launch_field_primitives(int C, const double* U, double* W, cudaStream_t stream);
+// apply_cell_flux and update on host-layout arrays (n cells / n values).
+cudaError_t launch_op_apply_cell_flux(int n, double dt, const double* vol, const double* flux, double* res,
+                                      cudaStream_t stream);
+cudaError_t launch_op_rk_update(long long n, double alpha, const double* res, const double* src, double* dst,
+                                cudaStream_t stream);
+
 // FP64 issue-rate kernel: blocks x 256 threads, 4 chains of iters operations
 // each (op 0 add, 1 multiply, 2 fused multiply-add); out holds one double per thread.
 cudaError_t launch_fp64_rate(int op, int blocks, int iters, double* out, cudaStream_t stream);

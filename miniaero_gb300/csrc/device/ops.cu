@@ -64,6 +64,55 @@ __global__ void k_op_primitives(int n, const double* U, double* V) {
   primitives(U + 5 * i, V + 5 * i);
 }
 
+// Each cell's boundary-face contributions summed in its residual list order
+// (boundary sets grouped Extrapolate, Tangent, NoSlip, Inflow), from +0 as
+// zero_cell_flux leaves the accumulator: out [5][C].
+__global__ void k_bc_gather(TopoView t, const double* __restrict__ fflux, double* __restrict__ out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= t.C) return;
+  const int C = t.C;
+  double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int s = 0; s < kMaxCellFaces; ++s) {
+    const int code = t.csr_flux[s * C + c];
+    if (code < 0) continue;
+    const int f = code >> 1;
+    if (f < t.Fi) continue;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) acc[k] += fflux[static_cast<size_t>(f) * 5 + k];
+  }
+#pragma unroll
+  for (int k = 0; k < 5; ++k) out[k * C + c] = acc[k];
+}
+
+// W = ComputePrimitives(U) per cell on [5][C] arrays (U as given, no stage update).
+__global__ void k_field_primitives(int C, const double* __restrict__ U, double* __restrict__ W) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  double u[5], v[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) u[k] = U[k * C + c];
+  primitives(u, v);
+#pragma unroll
+  for (int k = 0; k < 5; ++k) W[k * C + c] = v[k];
+}
+
+// apply_cell_flux (Flux.h:188-229) on host-layout arrays: res = 0 + (dt/V) flux.
+__global__ void k_op_apply_cell_flux(int n, double dt, const double* __restrict__ vol, const double* __restrict__ flux,
+                                     double* __restrict__ res) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const double dtv = dt / vol[c];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) res[5 * c + k] = 0.0 + dtv * flux[5 * c + k];
+}
+
+// update (TimeSolverExplicitRK4.h:106-128): dst = src + alpha * res.
+__global__ void k_op_rk_update(long long n, double alpha, const double* __restrict__ res,
+                               const double* __restrict__ src, double* __restrict__ dst) {
+  const long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (i < n) dst[i] = src[i] + alpha * res[i];
+}
+
 __device__ __forceinline__ uint64_t splitmix64(uint64_t& s) {
   uint64_t z = (s += 0x9E3779B97F4A7C15ull);
   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -235,6 +284,33 @@ cudaError_t launch_op_primitives(int n, const double* U, double* V, cudaStream_t
 cudaError_t launch_check_division(int mode, unsigned long long n, unsigned long long seed,
                                   unsigned long long* mismatches, double* example, cudaStream_t stream) {
   k_check_division<<<152 * 8, 256, 0, stream>>>(mode, n, seed, mismatches, example);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bc_gather(const TopoView& t, const double* fflux, double* out, cudaStream_t stream) {
+  if (t.C <= 0) return cudaSuccess;
+  k_bc_gather<<<blocks_for(t.C, 256), 256, 0, stream>>>(t, fflux, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_field_primitives(int C, const double* U, double* W, cudaStream_t stream) {
+  if (C <= 0) return cudaSuccess;
+  k_field_primitives<<<blocks_for(C, 256), 256, 0, stream>>>(C, U, W);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_op_apply_cell_flux(int n, double dt, const double* vol, const double* flux, double* res,
+                                      cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  k_op_apply_cell_flux<<<blocks_for(n, 256), 256, 0, stream>>>(n, dt, vol, flux, res);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_op_rk_update(long long n, double alpha, const double* res, const double* src, double* dst,
+                                cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  const long long blocks = (n + 255) / 256;
+  k_op_rk_update<<<static_cast<unsigned>(blocks), 256, 0, stream>>>(n, alpha, res, src, dst);
   return cudaGetLastError();
 }
 

@@ -986,6 +986,117 @@ extern "C" ma_status ma_debug_fp64_rate(int32_t op, double* inst_per_s) {
   return MA_OK;
 }
 
+namespace {
+
+// One RK stage's drivers taken one at a time on a state U (the operator
+// entry points below): U to the device as [5][C], W = primitives(U), and
+// the work arrays of one stage.
+struct FieldRun {
+  DevBufs b;
+  dev::StateBuffers st;
+  dev::StageBuffers<double> sb;
+};
+
+ma_status field_setup(ma_mesh* m, const double* U, int32_t layout, FieldRun& r) {
+  if (layout != MA_LAYOUT_AOS && layout != MA_LAYOUT_SOA) return set_error(MA_EINVAL, "bad state layout");
+  const size_t C = static_cast<size_t>(m->topo.C), F = static_cast<size_t>(m->topo.F);
+  std::vector<double> soa(5 * C);
+  for (size_t c = 0; c < C; ++c)
+    for (size_t k = 0; k < 5; ++k) soa[k * C + c] = layout == MA_LAYOUT_AOS ? U[5 * c + k] : U[k * C + c];
+  MA_CUDA_TRY(cudaSetDevice(m->device));
+  MA_CUDA_TRY(r.b.in(soa.data(), 5 * C, &r.st.Un));
+  r.st.Unp1 = r.st.Un;
+  MA_CUDA_TRY(r.b.in(nullptr, 5 * C, &r.sb.W));
+  MA_CUDA_TRY(r.b.in(nullptr, 15 * C, &r.sb.grad));
+  MA_CUDA_TRY(r.b.in(nullptr, 5 * C, &r.sb.phi));
+  MA_CUDA_TRY(r.b.in(nullptr, 5 * F, &r.sb.fflux));
+  MA_CUDA_TRY(dev::launch_field_primitives(m->topo.C, r.st.Un, r.sb.W, 0));
+  return MA_OK;
+}
+
+// [n][C] device array -> host [C][n] (the reference's LayoutRight views).
+ma_status download_cell_major(const double* d, size_t C, size_t n, double* out) {
+  std::vector<double> h(n * C);
+  MA_CUDA_TRY(cudaMemcpy(h.data(), d, sizeof(double) * n * C, cudaMemcpyDeviceToHost));
+  for (size_t c = 0; c < C; ++c)
+    for (size_t j = 0; j < n; ++j) out[c * n + j] = h[j * C + c];
+  return MA_OK;
+}
+
+}  // namespace
+
+extern "C" ma_status ma_op_green_gauss(ma_mesh* mesh, const double* U, int32_t layout, double* grad) {
+  if (!mesh || !U || !grad) return set_error(MA_EINVAL, "ma_op_green_gauss: null argument");
+  FieldRun r;
+  ma_status st = field_setup(mesh, U, layout, r);
+  if (st != MA_OK) return st;
+  dev::PathConfig cfg;
+  cfg.viscous = true;  // the sweep's gradient-only form
+  MA_CUDA_TRY(dev::launch_stage<double>(mesh->topo, mesh->g64, cfg, r.st, r.sb, 0, 0, dev::kSweep1));
+  return download_cell_major(r.sb.grad, mesh->topo.C, 15, grad);
+}
+
+extern "C" ma_status ma_op_stencil_limiter(ma_mesh* mesh, int32_t limiter, const double* U, int32_t layout,
+                                           double* phi) {
+  if (!mesh || !U || !phi) return set_error(MA_EINVAL, "ma_op_stencil_limiter: null argument");
+  if (limiter != MA_LIMITER_VENKAT && limiter != MA_LIMITER_VANALBADA) return set_error(MA_EINVAL, "bad limiter");
+  FieldRun r;
+  ma_status st = field_setup(mesh, U, layout, r);
+  if (st != MA_OK) return st;
+  dev::PathConfig cfg;
+  cfg.second_order = true;
+  cfg.viscous = true;
+  cfg.limiter = limiter;
+  MA_CUDA_TRY(dev::launch_stage<double>(mesh->topo, mesh->g64, cfg, r.st, r.sb, 0, 0, dev::kSweep1));
+  return download_cell_major(r.sb.phi, mesh->topo.C, 5, phi);
+}
+
+extern "C" ma_status ma_op_bc_flux(ma_mesh* mesh, const ma_options* o, const double* U, int32_t layout,
+                                   double* cell_flux) {
+  if (!mesh || !o || !U || !cell_flux) return set_error(MA_EINVAL, "ma_op_bc_flux: null argument");
+  if (o->viscosity_model != MA_VISC_SUTHERLAND && o->viscosity_model != MA_VISC_CONSTANT)
+    return set_error(MA_EINVAL, "bad viscosity model");
+  FieldRun r;
+  ma_status st = field_setup(mesh, U, layout, r);
+  if (st != MA_OK) return st;
+  dev::PathConfig cfg;
+  cfg.transport = dev::make_transport(o->viscosity_model, o->mu, o->prandtl);
+  for (int k = 0; k < 5; ++k) cfg.inflow[k] = o->inflow_state[k];
+  MA_CUDA_TRY(dev::launch_stage<double>(mesh->topo, mesh->g64, cfg, r.st, r.sb, 0, 0, dev::kBcFlux));
+  double* out;
+  MA_CUDA_TRY(r.b.in(nullptr, 5 * static_cast<size_t>(mesh->topo.C), &out));
+  MA_CUDA_TRY(dev::launch_bc_gather(mesh->topo, r.sb.fflux, out, 0));
+  return download_cell_major(out, mesh->topo.C, 5, cell_flux);
+}
+
+extern "C" ma_status ma_op_apply_cell_flux(int32_t ncells, double dt, const double* volumes, const double* cell_flux,
+                                           double* res) {
+  if (ncells < 0 || (ncells > 0 && (!volumes || !cell_flux || !res)))
+    return set_error(MA_EINVAL, "ma_op_apply_cell_flux: bad arguments");
+  if (ncells == 0) return MA_OK;
+  DevBufs b;
+  double *dv, *df, *dr;
+  MA_CUDA_TRY(b.in(volumes, static_cast<size_t>(ncells), &dv));
+  MA_CUDA_TRY(b.in(cell_flux, 5 * static_cast<size_t>(ncells), &df));
+  MA_CUDA_TRY(b.in(nullptr, 5 * static_cast<size_t>(ncells), &dr));
+  MA_CUDA_TRY(dev::launch_op_apply_cell_flux(ncells, dt, dv, df, dr, 0));
+  MA_CUDA_TRY(cudaMemcpy(res, dr, sizeof(double) * 5 * static_cast<size_t>(ncells), cudaMemcpyDeviceToHost));
+  return MA_OK;
+}
+
+extern "C" ma_status ma_op_rk_update(int64_t n, double alpha, const double* res, const double* src, double* dst) {
+  if (n < 0 || (n > 0 && (!res || !src || !dst))) return set_error(MA_EINVAL, "ma_op_rk_update: bad arguments");
+  if (n == 0) return MA_OK;
+  DevBufs b;
+  double *dr, *ds, *dd;
+  MA_CUDA_TRY(b.in(res, static_cast<size_t>(n), &dr));
+  MA_CUDA_TRY(b.in(src, static_cast<size_t>(n), &ds));
+  MA_CUDA_TRY(b.in(nullptr, static_cast<size_t>(n), &dd));
+  MA_CUDA_TRY(dev::launch_op_rk_update(n, alpha, dr, ds, dd, 0));
+  MA_CUDA_TRY(cudaMemcpy(dst, dd, sizeof(double) * static_cast<size_t>(n), cudaMemcpyDeviceToHost));
+  return MA_OK;
+}
+
 extern "C" ma_status ma_op_primitives(int32_t n, const double* U, double* V) {
   if (n < 0 || (n > 0 && (!U || !V))) return set_error(MA_EINVAL, "ma_op_primitives: bad arguments");
   if (n == 0) return MA_OK;

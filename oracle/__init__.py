@@ -59,6 +59,9 @@ def lib():
         L.oracle_step.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.oracle_get_state.argtypes = [ctypes.c_void_p, P_f64, P_f64]
         L.oracle_free.argtypes = [ctypes.c_void_p]
+        for name in ("oracle_field_gradients", "oracle_field_limiter", "oracle_field_bc_flux"):
+            getattr(L, name).argtypes = [ctypes.POINTER(oracle_mesh), ctypes.POINTER(oracle_options), P_f64, P_f64]
+            getattr(L, name).restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -207,3 +210,28 @@ def primitives(U):
     for i in range(U.shape[0]):
         L.oracle_primitives(_p(U[i], P_f64), _p(out[i], P_f64))
     return out
+
+
+def _field(fn, md, options, U, width):
+    om = OracleMesh(md)
+    o = _c_options(options)
+    U = np.ascontiguousarray(U, dtype=np.float64).reshape(md.ncells, 5)
+    out = np.empty((md.ncells, width))
+    if getattr(lib(), fn)(ctypes.byref(om.c), ctypes.byref(o), _p(U, P_f64), _p(out, P_f64)) != 0:
+        raise RuntimeError(fn + " failed")
+    return out
+
+
+def field_gradients(md, options, U):
+    """GreenGauss::compute_gradients on state U: (ncells, 5, 3)."""
+    return _field("oracle_field_gradients", md, options, U, 15).reshape(md.ncells, 5, 3)
+
+
+def field_limiter(md, options, U):
+    """compute_min_max + compute_limiter (options.limiter) on U: (ncells, 5)."""
+    return _field("oracle_field_limiter", md, options, U, 5)
+
+
+def field_bc_flux(md, options, U):
+    """The BC functors in Solve's order on U: boundary part of cell_flux, (ncells, 5)."""
+    return _field("oracle_field_bc_flux", md, options, U, 5)

@@ -781,3 +781,54 @@ void oracle_init_constant(const oracle_mesh* m, const double st[5], double* U) {
   for (int i = 0; i < m->ncells; ++i)
     for (int k = 0; k < 5; ++k) U[5 * i + k] = st[k];
 }
+
+/* ---- drivers one at a time (unit parity of the device operator entry points) ---- */
+static const int bc_type_order[4] = {0, 1, 3, 2};  /* Extrapolate, Tangent, NoSlip, Inflow */
+
+static oracle_state* field_state(const oracle_mesh* m, const oracle_options* o, oracle_options* serial,
+                                 const double* U) {
+  *serial = *o;
+  serial->cell_flux = 0;
+  oracle_state* h = oracle_create(m, serial, U, 1);
+  if (!h) return NULL;
+  memcpy(h->s.Utmp, U, sizeof(double) * 5 * (size_t)m->ncells);
+  zero_cell_flux(&h->s);
+  return h;
+}
+
+/* GreenGauss::compute_gradients (GreenGauss.h:300-321) */
+int oracle_field_gradients(const oracle_mesh* m, const oracle_options* o, const double* U, double* grad) {
+  oracle_options so;
+  oracle_state* h = field_state(m, o, &so, U);
+  if (!h) return 1;
+  green_gauss(&h->s);
+  memcpy(grad, h->s.grad, sizeof(double) * 15 * (size_t)m->ncells);
+  oracle_free(h);
+  return 0;
+}
+
+/* StencilLimiter::compute_min_max + compute_limiter (StencilLimiter.h:532-616) */
+int oracle_field_limiter(const oracle_mesh* m, const oracle_options* o, const double* U, double* phi) {
+  oracle_options so;
+  oracle_state* h = field_state(m, o, &so, U);
+  if (!h) return 1;
+  green_gauss(&h->s);
+  min_max(&h->s);
+  limiter(&h->s);
+  memcpy(phi, h->s.lim, sizeof(double) * 5 * (size_t)m->ncells);
+  oracle_free(h);
+  return 0;
+}
+
+/* The BC functors in Solve's order (TimeSolverExplicitRK4.h:428-475) */
+int oracle_field_bc_flux(const oracle_mesh* m, const oracle_options* o, const double* U, double* cell_flux) {
+  oracle_options so;
+  oracle_state* h = field_state(m, o, &so, U);
+  if (!h) return 1;
+  for (int t = 0; t < 4; ++t)
+    for (int b = 0; b < m->nbc; ++b)
+      if (m->bc[b].type == bc_type_order[t]) bc_flux(&h->s, &m->bc[b]);
+  memcpy(cell_flux, h->s.cell_flux, sizeof(double) * 5 * (size_t)m->ncells);
+  oracle_free(h);
+  return 0;
+}

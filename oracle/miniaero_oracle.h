@@ -86,6 +86,14 @@ double oracle_venkat(double dumax, double dumin, double du, double deltax2);
 double oracle_vanalbada(double dumax, double dumin, double du);
 void oracle_primitives(const double* U, double* V);
 
+/* One RK stage's drivers taken one at a time on a state U ([ncells*5]; the
+ * stage state U_tmp of Solve), in the serial ATOMICS_FLUX order. Return 0 on
+ * success. grad [ncells*15] (cell, component, direction), phi and cell_flux
+ * [ncells*5]. */
+int oracle_field_gradients(const oracle_mesh* mesh, const oracle_options* opts, const double* U, double* grad);
+int oracle_field_limiter(const oracle_mesh* mesh, const oracle_options* opts, const double* U, double* phi);
+int oracle_field_bc_flux(const oracle_mesh* mesh, const oracle_options* opts, const double* U, double* cell_flux);
+
 #ifdef __cplusplus
 }
 #endif

@@ -261,3 +261,50 @@ def test_fp64_rate_is_measured(has_gpu):
     from miniaero_gb300 import _lib
     with pytest.raises(ma.MiniaeroError):
         _lib.check(_lib.lib().ma_debug_fp64_rate(3, ctypes.byref(ctypes.c_double())))
+
+
+# ---- one stage's drivers taken one at a time (ma_op_green_gauss, ...) ---------------
+@pytest.mark.parametrize("name", sorted(REF_TESTS))
+def test_stage_drivers_one_at_a_time_bitexact(has_gpu, name):
+    """Green-Gauss gradients, both limiters, the boundary functors,
+    apply_cell_flux and update on an evolved state of each reference case,
+    bit for bit against the oracle's drivers (and IEEE numpy for the two
+    elementwise ones)."""
+    import ctypes
+    from miniaero_gb300 import _lib
+    o = make_options(*REF_TESTS[name])
+    md = ma.Parallel3DMesh.from_options(o).fill_mesh_data()
+    U = oracle.solve(md, o, ma.initial_state(md, o), nsteps=5)
+    dm = ma.DeviceMesh(md)
+    assert_bitexact(ma.green_gauss(dm, U).reshape(-1, 5), oracle.field_gradients(md, o, U).reshape(-1, 5))
+    soa = np.ascontiguousarray(U.T)
+    g = np.empty((md.ncells, 5, 3))
+    _lib.check(_lib.lib().ma_op_green_gauss(dm._h, _lib.f64p(soa), ma.MA_LAYOUT_SOA, _lib.f64p(g)))
+    assert_bitexact(g.reshape(-1, 5), oracle.field_gradients(md, o, U).reshape(-1, 5))
+    for lim in (ma.MA_LIMITER_VENKAT, ma.MA_LIMITER_VANALBADA):
+        ol = o.copy()
+        ol.limiter = lim
+        assert_bitexact(ma.stencil_limiter(dm, U, lim), oracle.field_limiter(md, ol, U))
+    flux = ma.bc_flux(dm, o, U)
+    assert_bitexact(flux, oracle.field_bc_flux(md, o, U))
+    res = ma.apply_cell_flux(o.dt, md.cell_volumes, flux)
+    assert_bitexact(res, 0.0 + (o.dt / md.cell_volumes)[:, None] * flux)
+    assert_bitexact(ma.rk_update(0.5, res, U), U + 0.5 * res)
+    dm.close()
+
+
+def test_stage_drivers_reject_bad_arguments(has_gpu):
+    import ctypes
+    from miniaero_gb300 import _lib
+    o = make_options(0, (1.0, 0.5, 0.5, 0.0), (4, 2, 2), 1, 1e-6, 1, 1)
+    md = ma.Parallel3DMesh.from_options(o).fill_mesh_data()
+    dm = ma.DeviceMesh(md)
+    U = ma.initial_state(md, o)
+    with pytest.raises(ma.MiniaeroError):
+        ma.stencil_limiter(dm, U, 7)
+    g = np.empty((md.ncells, 5, 3))
+    with pytest.raises(ma.MiniaeroError):
+        _lib.check(_lib.lib().ma_op_green_gauss(dm._h, _lib.f64p(np.ascontiguousarray(U)), 9, _lib.f64p(g)))
+    with pytest.raises(ma.MiniaeroError):
+        _lib.check(_lib.lib().ma_op_rk_update(-1, 1.0, _lib.f64p(g), _lib.f64p(g), _lib.f64p(g)))
+    dm.close()

@@ -218,7 +218,8 @@ extern "C" ma_status ma_batch_create(const ma_options* o, int32_t capacity, size
   *out = nullptr;
   if (o->precision != MA_PREC_FP64 && o->precision != MA_PREC_MIXED) return set_error(MA_EINVAL, "bad precision");
   if (o->gather != MA_GATHER_ATOMICS && o->gather != MA_GATHER_CELL_FLUX) return set_error(MA_EINVAL, "bad gather");
-  std::unique_ptr<ma_batch> b(new (std::nothrow) ma_batch);
+  // A failure part way releases what was created (ma_batch_free skips null handles).
+  std::unique_ptr<ma_batch, void (*)(ma_batch*)> b(new (std::nothrow) ma_batch, ma_batch_free);
   if (!b) return set_error(MA_ENOMEM, "ma_batch_create: out of host memory");
   b->opts = *o;
   b->mixed = o->precision == MA_PREC_MIXED;

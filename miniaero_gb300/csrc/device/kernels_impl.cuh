@@ -656,11 +656,8 @@ __global__ void __launch_bounds__(kCellBlock) k_residual(TopoView t, const R* __
 // Each block takes whole chunks; a chunk holds blockDim.x consecutive items of
 // one segment. The chunk count is read from device memory so that a captured
 // graph stays valid when the batch membership changes.
-// Batched sweep: at most 256 threads a block; FP64 at 2 blocks per SM like the
-// single-mesh sweep, FP32 at 4 (64 registers), where the contracted FP32 code
-// would otherwise take 66 registers and drop to 3 blocks.
 template <class R, int MODE>
-__global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 4) kb_sweep1(const Segment<R>* __restrict__ segs, const int2* __restrict__ chunks,
+__global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 0) kb_sweep1(const Segment<R>* __restrict__ segs, const int2* __restrict__ chunks,
                                                  const int* __restrict__ nchunks) {
   const int n = *nchunks;
   for (int ch = blockIdx.x; ch < n; ch += gridDim.x) {

@@ -1,8 +1,7 @@
 // Mixed form: FP32 face flux, gradient and limiter; FP64 residual
-// accumulation and RK4 update. Built with --fmad=true: nothing here has
-// reference bits to keep, and the fused forms are shorter and more accurate.
-// The single-mesh and the batched kernels inline the same expression trees,
-// so a solve gives identical bits alone or batched.
+// accumulation and RK4 update. Built with --fmad=false like the FP64 form:
+// without contraction every item's arithmetic is the same in the single-mesh
+// and the batched kernels, so a solve gives identical bits alone or batched.
 #include "kernels_impl.cuh"
 
 namespace miniaero {

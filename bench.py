@@ -607,20 +607,25 @@ def run_serving(ma, n_requests=32, rate=200.0, nsteps=500, seed=1, budget=150 <<
     """Serving stream: Poisson arrivals (rate/s, seeded) of flat-plate solves,
     Mach uniform in [0.1, 0.6], sizes from {32,48,64,96,128}^3, nsteps RK4
     steps each, mixed precision, admitted under the HBM budget with at most
-    max_running_cells cells running at once (enough to fill the GPU)."""
+    max_running_cells cells running at once (enough to fill the GPU). The
+    server runs its batch with the launch shapes the autotuner picked for the
+    same requests as one static batch (tuned once for the workload, before
+    the stream starts)."""
     rng = np.random.default_rng(seed)
     sizes = [32, 48, 64, 96, 128]
     phys = ma.Options(problem_type=1, second_order_space=1, viscous=1, limiter=ma.MA_LIMITER_VANALBADA,
                       viscosity_model=ma.MA_VISC_CONSTANT, mu=1.8e-5, prandtl=0.72, precision=ma.MA_PREC_MIXED,
                       cfl=0.5)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_requests))
+    reqs = [(float(a), int(rng.choice(sizes)), float(rng.uniform(0.1, 0.6))) for a in arrivals]
+    static = run_static_batch(ma, phys, reqs, budget)
     srv = ma.Server(phys, budget_bytes=budget, tick_steps=tick, capacity=512, thread=True)
     srv.set_max_running_cells(max_running_cells)
+    srv.set_launch(*static["launch"])
     t0 = time.perf_counter()
     for n in sizes:  # mesh cache warm-up: one device mesh per size
         srv.preload(ma.Server.request(n, n, n, 2.0, 0.5, 0.5, flat_plate_inflow(0.3), nsteps))
     setup_s = time.perf_counter() - t0
-    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_requests))
-    reqs = [(float(a), int(rng.choice(sizes)), float(rng.uniform(0.1, 0.6))) for a in arrivals]
     ids = []
     start = time.perf_counter()
     for at, n, mach in reqs:
@@ -639,10 +644,10 @@ def run_serving(ma, n_requests=32, rate=200.0, nsteps=500, seed=1, budget=150 <<
     done = sum(1 for i in infos if i.state == 2)
     cell_stages = sum(i.cells * 4 * nsteps for i in infos if i.state == 2)
     offered = sum(n ** 3 * 4 * nsteps for _, n, _ in reqs) / (reqs[-1][0] if reqs[-1][0] > 0 else 1.0)
-    static = run_static_batch(ma, phys, reqs, budget)
     return {"workload": "Poisson %.0f/s flat-plate requests, Mach U[0.1,0.6], sizes {32..128}^3, %d steps, mixed"
                         % (rate, nsteps),
             "requests": n_requests, "completed": done, "tick_steps": tick, "budget_bytes": budget,
+            "launch": {"block": static["launch"][0], "grid": static["launch"][1]},
             "max_running_cells": max_running_cells,
             "mesh_cache_setup_s": setup_s,
             "throughput": {"value": cell_stages / wall / 1e6, "unit": "Mcell-stage/s (wall, first arrival to last)"},
@@ -679,6 +684,7 @@ def run_static_batch(ma, phys, reqs, budget, steps=40, warmup=3):
         b.add(dm, ma.initial_state(md, o), inflow_state=flat_plate_inflow(mach))
         cells += md.ncells
     b.autotune(reps=2)
+    launch = b.launch
     b.step(warmup)
     b.synchronize()
     stream = torch.cuda.ExternalStream(b.stream)
@@ -692,7 +698,7 @@ def run_static_batch(ma, phys, reqs, budget, steps=40, warmup=3):
     for md, dm in meshes.values():
         dm.close()
     return {"value": cells * 4 * steps / (ms / 1e3) / 1e6, "unit": "Mcell-stage/s", "members": len(reqs),
-            "cells": cells, "timed_steps": steps}
+            "cells": cells, "timed_steps": steps, "launch": launch}
 
 
 def main():

@@ -329,6 +329,10 @@ void ma_server_free(ma_server* s);
 /* Admission cap on the cells of running requests (0 = none; default). A
  * request larger than the cap still runs when nothing else does. */
 ma_status ma_server_set_max_running_cells(ma_server* s, int64_t cells);
+/* Launch shapes of the server's batch (as ma_batch_set_launch), e.g. the ones
+ * ma_batch_autotune found for the workload; only while no request is queued
+ * or running (MA_ESTATE otherwise). */
+ma_status ma_server_set_launch(ma_server* s, const int32_t* block, const int32_t* grid);
 /* Thread-safe; returns at once with the request id. */
 ma_status ma_server_submit(ma_server* s, const ma_request* r, int64_t* id);
 /* Builds and caches the device mesh a request of this shape would use. */

@@ -508,6 +508,12 @@ class Server:
     def set_max_running_cells(self, cells):
         check(lib().ma_server_set_max_running_cells(self._h, int(cells)))
 
+    def set_launch(self, block, grid):
+        """Launch shapes of the server's batch (e.g. from Batch.autotune); only while idle."""
+        b = np.ascontiguousarray(block, dtype=np.int32)
+        g = np.ascontiguousarray(grid, dtype=np.int32)
+        check(lib().ma_server_set_launch(self._h, i32p(b), i32p(g)))
+
     def preload(self, req):
         check(lib().ma_server_preload_mesh(self._h, ctypes.byref(req)))
 

@@ -208,6 +208,7 @@ _SIGNATURES = {
                                    ctypes.POINTER(c_void_p)]),
     "ma_server_free": (None, [c_void_p]),
     "ma_server_submit": (c_int32, [c_void_p, ctypes.POINTER(ma_request), ctypes.POINTER(ctypes.c_int64)]),
+    "ma_server_set_launch": (c_int32, [c_void_p, P_i32, P_i32]),
     "ma_server_set_max_running_cells": (c_int32, [c_void_p, ctypes.c_int64]),
     "ma_server_preload_mesh": (c_int32, [c_void_p, ctypes.POINTER(ma_request)]),
     "ma_server_poll": (c_int32, [c_void_p, P_i32]),

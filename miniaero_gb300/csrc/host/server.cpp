@@ -411,6 +411,23 @@ extern "C" ma_status ma_server_set_max_running_cells(ma_server* s, int64_t cells
   return MA_OK;
 }
 
+extern "C" ma_status ma_server_set_launch(ma_server* s, const int32_t* block, const int32_t* grid) {
+  if (!s || !block || !grid) return set_error(MA_EINVAL, "ma_server_set_launch: null argument");
+  std::lock_guard<std::mutex> g(s->mu);
+  // The batch steps with the lock released: its launch shapes change only
+  // while no request is queued or running.
+  if (!s->queue.empty()) return set_error(MA_ESTATE, "ma_server_set_launch: requests are queued");
+  for (auto& kv : s->reqs)
+    if (kv.second.state == MA_REQ_RUNNING) return set_error(MA_ESTATE, "ma_server_set_launch: requests are running");
+  if (s->dry) {
+    for (int k = 0; k < 4; ++k)
+      if (block[k] < 32 || block[k] > 256 || block[k] % 32 || grid[k] < 1 || grid[k] > 65535)
+        return set_error(MA_EINVAL, "ma_server_set_launch: block must be 32..256 in steps of 32, grid 1..65535");
+    return MA_OK;
+  }
+  return ma_batch_set_launch(s->batch, block, grid);
+}
+
 extern "C" ma_status ma_server_submit(ma_server* s, const ma_request* r, int64_t* id) {
   if (!s || !r || !id) return set_error(MA_EINVAL, "ma_server_submit: null argument");
   if (r->nx < 1 || r->ny < 1 || r->nz < 1 || r->nsteps < 0)

@@ -168,3 +168,19 @@ def test_thread_mode_serves_and_bounded_wait():
     s.cancel(a)
     assert s.wait(b, timeout=10.0).state == s.DONE
     s.close()
+
+
+def test_launch_shapes_change_only_while_idle():
+    s = server(budget=1 << 30)
+    s.set_launch([256, 64, 128, 64], [1216, 2432, 2432, 2432])
+    with pytest.raises(ma.MiniaeroError):
+        s.set_launch([300, 64, 128, 64], [1216, 2432, 2432, 2432])
+    rid = s.submit(req(16, steps=30))
+    with pytest.raises(ma.MiniaeroError) as e:
+        s.set_launch([128] * 4, [1216] * 4)
+    assert e.value.status == ma._lib.MA_ESTATE
+    while s.poll():
+        pass
+    assert s.query(rid).state == s.DONE
+    s.set_launch([128] * 4, [1216] * 4)
+    s.close()

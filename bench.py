@@ -59,7 +59,7 @@ WORKLOADS = {
 DEFAULT_WORKLOAD = "sod_2nd_viscous_256x128x128"
 
 
-def kernel_bytes(md, kind, w):
+def kernel_bytes(md, kind, w, second_viscous=True):
     """Algorithmic (compulsory) DRAM bytes of one launch: every array the
     kernel touches read or written once, neighbour data counted once (w =
     bytes of the flux/gradient type). Second-order viscous form on axis-aligned
@@ -74,7 +74,8 @@ def kernel_bytes(md, kind, w):
         # one area component and the offset of each side.
         return C * (5 * w + 8 + 8 + 72 + 1 + 15 * w + 5 * w) + Fi * 3 * w + Fb * 2 * w
     if kind == "internal_face_flux":
-        return Fi * (8 + 7 * w + 5 * w) + C * 25 * w
+        # W, grad and phi of both cells; W only in the first-order inviscid form.
+        return Fi * (8 + 7 * w + 5 * w) + C * (25 if second_viscous else 5) * w
     if kind == "boundary_face_flux":
         return Fb * (4 + 16 * w + 5 * w) + Fb * 5 * w
     if kind == "residual_rk_update":
@@ -120,14 +121,18 @@ def fp64_ceiling(kernel, rates):
     return n / (f / rates["fma"] + (n - f) / addmul)
 
 
-def kernel_rooflines(md, prof, w, sm_mhz, fp64_rates=None):
+def kernel_rooflines(md, prof, w, sm_mhz, fp64_rates=None, counted=True, second_viscous=True, traffic_key=None):
     """Per-kernel time share, achieved algorithmic GB/s and, where the ncu
     summary gives FP64 instructions per item, FP64-pipe throughput against
     the nominal 2 per SM per clock and against the rates measured on this
-    device (fp64_rates: {"add", "mul", "fma"} thread instructions/s)."""
+    device (fp64_rates: {"add", "mul", "fma"} thread instructions/s).
+    counted: the workload has the physics the per-item counts were captured
+    on (Sod, second order, viscous, Venkatakrishnan); otherwise no FP64
+    fractions are reported. traffic_key: the ncu summary's table of DRAM
+    bytes per launch when it was scaled to this workload, else None."""
     total_ms = sum(v[0] for v in prof.values())
     peak, peak_kind = load_peaks()
-    fp64 = load_traffic("fp64_thread_inst_per_item") or {}
+    fp64 = (load_traffic("fp64_thread_inst_per_item") or {}) if counted else {}
     items = {"sweep_gradient_limiter": md.ncells, "internal_face_flux": md.internal.nfaces,
              "boundary_face_flux": sum(b.nfaces for b in md.bc), "residual_rk_update": md.ncells}
     clock = (sm_mhz or 2070.0) * 1e6
@@ -135,7 +140,7 @@ def kernel_rooflines(md, prof, w, sm_mhz, fp64_rates=None):
     kernels = {}
     for k, (ms, n) in prof.items():
         per = ms / n
-        b = kernel_bytes(md, k, w)
+        b = kernel_bytes(md, k, w, second_viscous)
         e = {"ms_per_launch": per, "launches": n, "share": ms / total_ms, "algorithmic_bytes": b,
              "achieved_GBps": b / (per / 1e3) / 1e9}
         if w == 8 and k in fp64:
@@ -149,7 +154,7 @@ def kernel_rooflines(md, prof, w, sm_mhz, fp64_rates=None):
     d = kernels[dom]
     roofline = {"kernel": dom, "bound": "hbm", "achieved": d["achieved_GBps"], "peak": peak,
                 "peak_source": peak_kind, "unit": "GB/s", "frac": d["achieved_GBps"] / peak,
-                "traffic": (load_traffic("traffic_bytes_per_launch") or {}).get(dom),
+                "traffic": (load_traffic(traffic_key) or {}).get(dom) if traffic_key else None,
                 "algorithmic_bytes_per_launch": d["algorithmic_bytes"], "ms_per_launch": d["ms_per_launch"]}
     if "fp64_pipe_frac" in d:
         roofline["fp64_pipe"] = {"frac": d["fp64_pipe_frac"], "peak_inst_per_s": fp64_peak,
@@ -412,8 +417,15 @@ def run_ours(args, world, rank, local):
     prof = solver.profile_steps(max(2, min(args.steps, 10)))
     Fi = md.internal.nfaces
     fp64_rates = {op: ma.fp64_rate(op) for op in ("add", "mul", "fma")}
-    roofline, kernels = kernel_rooflines(md, prof, 8, clocks.get("sm_mhz"), fp64_rates)
-    roofline["stage"] = stage_roofline(C, prof, 8)
+    # The ncu per-item FP64 counts and the two-sweep stage model are for the
+    # second-order viscous path; the counts were captured on the Sod workloads.
+    wl = WORKLOADS[name]
+    second_viscous = bool(wl.get("second_order_space") and wl.get("viscous"))
+    counted = name.startswith("sod_2nd_viscous")
+    scaled = name == DEFAULT_WORKLOAD  # the ncu traffic tables are scaled to this workload's launches
+    roofline, kernels = kernel_rooflines(md, prof, 8, clocks.get("sm_mhz"), fp64_rates, counted, second_viscous,
+                                         "traffic_bytes_per_launch" if scaled else None)
+    roofline["stage"] = stage_roofline(C, prof, 8) if second_viscous else None
 
     # ---- mixed form on the same mesh: throughput and error vs FP64 ----
     om = make_options(ma, name, "mixed")
@@ -438,9 +450,10 @@ def run_ours(args, world, rank, local):
     errs_mom = [float(np.linalg.norm(Um[:, k] - U_fp64[:, k]) / mom) for k in (1, 2, 3)]
     mprof = msolver.profile_steps(2)
     # FP32 work arrays: algorithmic bytes at 4 bytes per value, against HBM.
-    mroofline, mkernels = kernel_rooflines(md, mprof, 4, clocks.get("sm_mhz"))
-    mroofline["traffic"] = (load_traffic("traffic_bytes_per_launch_mixed") or {}).get(mroofline["kernel"])
-    mroofline["stage"] = stage_roofline(C, mprof, 4)
+    mroofline, mkernels = kernel_rooflines(md, mprof, 4, clocks.get("sm_mhz"), None, counted, second_viscous)
+    mroofline["traffic"] = ((load_traffic("traffic_bytes_per_launch_mixed") or {}).get(mroofline["kernel"])
+                            if scaled else None)
+    mroofline["stage"] = stage_roofline(C, mprof, 4) if second_viscous else None
     msolver.close()
 
     # ---- end to end through the C ABI with pinned host buffers ----

@@ -64,6 +64,7 @@ def build(verbose=False, ptxas_info=False):
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(ORACLE_BUILD, exist_ok=True)
     nvcc = _nvcc()
+    cuda_include = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), "include")  # NVTX headers
     jobs = []
     for src, extra in DEVICE_SOURCES:
         cmd = [nvcc] + NVCC_COMMON + extra + ["-c", os.path.join(CSRC, src), "-o", _obj(src)]
@@ -71,7 +72,7 @@ def build(verbose=False, ptxas_info=False):
             cmd += ["-Xptxas", "-v"]
         jobs.append(cmd)
     for src in HOST_SOURCES:
-        jobs.append(HOST_CXX + ["-c", os.path.join(CSRC, src), "-o", _obj(src)])
+        jobs.append(HOST_CXX + ["-I" + cuda_include, "-c", os.path.join(CSRC, src), "-o", _obj(src)])
     jobs.append(["gcc", "-O2", "-std=c11", "-fPIC", "-ffp-contract=off", "-fopenmp", "-shared",
                  os.path.join(ORACLE, "miniaero_oracle.c"), "-o", ORACLE_LIB, "-lm"])
     outputs = []
@@ -79,7 +80,7 @@ def build(verbose=False, ptxas_info=False):
         for out in ex.map(lambda c: _run(c, verbose), jobs):
             outputs.append(out)
     objs = [_obj(s) for s, _ in DEVICE_SOURCES] + [_obj(s) for s in HOST_SOURCES]
-    _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-cudart", "static", "-lpthread"], verbose)
+    _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-cudart", "static", "-lpthread", "-ldl"], verbose)
     _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", os.path.join(CSRC, "cli", "main.cpp"),
           "-o", CLI, "-L" + BUILD, "-lminiaero_gpu", "-Wl,-rpath,$ORIGIN"], verbose)
     if ptxas_info:

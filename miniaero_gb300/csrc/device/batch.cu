@@ -19,6 +19,7 @@
 
 #include "../../../include/miniaero_gpu.h"
 #include "../host/errors.hpp"
+#include "../host/trace.hpp"
 #include "batch_internal.hpp"
 #include "kernels.cuh"
 
@@ -380,6 +381,7 @@ extern "C" ma_status ma_batch_get_state(ma_batch* b, int32_t id, double* U, int3
 extern "C" ma_status ma_batch_step(ma_batch* b, int32_t nsteps) {
   if (!b || nsteps < 0) return set_error(MA_EINVAL, "ma_batch_step: bad arguments");
   if (nsteps == 0 || b->members.empty()) return MA_OK;
+  miniaero::TraceRange trace("ma_batch_step");
   if (b->tables_dirty) {
     ma_status st = upload_tables(b);
     if (st != MA_OK) return st;
@@ -505,6 +507,7 @@ extern "C" ma_status ma_batch_set_launch(ma_batch* b, const int32_t* block, cons
 extern "C" ma_status ma_batch_autotune(ma_batch* b, int32_t reps, double* best_ms) {
   if (!b || reps <= 0) return set_error(MA_EINVAL, "ma_batch_autotune: bad arguments");
   if (b->members.empty()) return set_error(MA_ESTATE, "ma_batch_autotune: empty batch");
+  miniaero::TraceRange trace("ma_batch_autotune");
   // Save U_n, U_np1 and W of every member (the leading region of its
   // allocation); tuning runs real stages, the other arrays are recomputed by
   // the next stage before they are read.

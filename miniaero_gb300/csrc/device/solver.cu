@@ -23,6 +23,7 @@
 #include "../../../include/miniaero_gpu.h"
 #include "../host/errors.hpp"
 #include "../host/parallel.hpp"
+#include "../host/trace.hpp"
 #include "batch_internal.hpp"
 #include "kernels.cuh"
 
@@ -147,6 +148,7 @@ extern "C" ma_status ma_mesh_upload_ex(const ma_mesh_view* v, int32_t flags, ma_
   if (flags & ~MA_MESH_CELL_FLUX) return set_error(MA_EINVAL, "ma_mesh_upload_ex: unknown flags");
   const bool cell_flux = (flags & MA_MESH_CELL_FLUX) != 0;
   *out = nullptr;
+  miniaero::TraceRange trace("ma_mesh_upload");
   ma_status st = validate_view(v);
   if (st != MA_OK) return st;
   try {
@@ -708,6 +710,7 @@ ma_status download(ma_solver* s, const double* src, double* U, int32_t layout) {
 
 extern "C" ma_status ma_solver_set_state(ma_solver* s, const double* U, int32_t layout) {
   if (!s || !U) return set_error(MA_EINVAL, "ma_solver_set_state: null argument");
+  miniaero::TraceRange trace("ma_solver_set_state");
   MA_CUDA_TRY(cudaSetDevice(s->mesh->device));
   ma_status st = upload_state(s, U, layout);
   if (st != MA_OK) return st;
@@ -748,6 +751,7 @@ extern "C" ma_status ma_solver_init_state(ma_solver* s, const ma_host_mesh* hm) 
 extern "C" ma_status ma_solver_get_state(ma_solver* s, double* U, int32_t layout) {
   if (!s || !U) return set_error(MA_EINVAL, "ma_solver_get_state: null argument");
   if (!s->state_set) return set_error(MA_ESTATE, "solver state has not been set");
+  miniaero::TraceRange trace("ma_solver_get_state");
   MA_CUDA_TRY(cudaSetDevice(s->mesh->device));
   return download(s, s->st.Un, U, layout);
 }
@@ -764,6 +768,7 @@ extern "C" ma_status ma_solver_step(ma_solver* s, int32_t nsteps) {
   if (nsteps < 0) return set_error(MA_EINVAL, "ma_solver_step: negative step count");
   if (!s->state_set) return set_error(MA_ESTATE, "solver state has not been set");
   if (nsteps == 0) return MA_OK;
+  miniaero::TraceRange trace("ma_solver_step");
   MA_CUDA_TRY(cudaSetDevice(s->mesh->device));
   if (!s->graph) {
     ma_status st = capture_step_graph(s);
@@ -777,6 +782,7 @@ extern "C" ma_status ma_solver_step(ma_solver* s, int32_t nsteps) {
 extern "C" ma_status ma_solver_profile_steps(ma_solver* s, int32_t nsteps, double* kernel_ms, int32_t* kernel_launches) {
   if (!s || nsteps < 0 || !kernel_ms || !kernel_launches) return set_error(MA_EINVAL, "ma_solver_profile_steps: bad arguments");
   if (!s->state_set) return set_error(MA_ESTATE, "solver state has not been set");
+  miniaero::TraceRange trace("ma_solver_profile_steps");
   MA_CUDA_TRY(cudaSetDevice(s->mesh->device));
   for (int k = 0; k < MA_PROFILE_KINDS; ++k) { kernel_ms[k] = 0.0; kernel_launches[k] = 0; }
   const dev::TopoView& t = s->topo;

@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "../../../include/miniaero_gpu.h"
+#include "trace.hpp"
 #include "errors.hpp"
 #include "mesh.hpp"
 
@@ -47,6 +48,7 @@ extern "C" const char* ma_status_string(ma_status s) {
 extern "C" ma_status ma_host_mesh_build(const ma_options* o, ma_host_mesh** out) {
   if (!o || !out) return set_error(MA_EINVAL, "ma_host_mesh_build: null argument");
   *out = nullptr;
+  miniaero::TraceRange trace("ma_host_mesh_build");
   miniaero::MeshSpec spec;
   spec.nx = o->nx; spec.ny = o->ny; spec.nz = o->nz;
   spec.lx = o->lx; spec.ly = o->ly; spec.lz = o->lz;

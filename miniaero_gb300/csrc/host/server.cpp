@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "../../../include/miniaero_gpu.h"
+#include "trace.hpp"
 #include "errors.hpp"
 
 using miniaero::set_error;
@@ -297,6 +298,7 @@ ma_status poll_locked(ma_server* s, std::unique_lock<std::mutex>& lk, int32_t* p
   ma_status st = MA_OK;
   if (!s->dry && n > 0) {
     lk.unlock();
+    miniaero::TraceRange trace("ma_server_tick");
     st = ma_batch_step(s->batch, n);
     if (st == MA_OK) st = ma_batch_synchronize(s->batch);
     lk.lock();

@@ -308,3 +308,28 @@ def test_stage_drivers_reject_bad_arguments(has_gpu):
     with pytest.raises(ma.MiniaeroError):
         _lib.check(_lib.lib().ma_op_rk_update(-1, 1.0, _lib.f64p(g), _lib.f64p(g), _lib.f64p(g)))
     dm.close()
+
+
+# ---- failure detection: bad states found by a device reduction (no trap) -----------
+def test_state_check_reports_the_first_bad_cell(has_gpu):
+    """Host-prepared states with a NaN, an infinity, a negative density or a
+    zero energy are reported as MA_ENUMERIC with the first bad cell; the
+    solver stays usable afterwards."""
+    o = make_options(0, (1.0, 0.5, 0.5, 0.0), (8, 4, 4), 2, 1e-6, 1, 1)
+    md = ma.Parallel3DMesh.from_options(o).fill_mesh_data()
+    U0 = ma.initial_state(md, o)
+    with ma.TimeSolverExplicitRK4(md, o) as s:
+        s.set_state(U0)
+        assert s.check_state() == (0, -1)
+        for cells, k, v in (([37], 2, np.nan), ([91, 12], 3, np.inf), ([60, 5], 0, -1.0), ([100], 4, 0.0)):
+            U = U0.copy()
+            for c in cells:
+                U[c, k] = v
+            s.set_state(U)
+            st, bad = s.check_state()
+            assert st == ma._lib.MA_ENUMERIC and bad == min(cells), (cells, k, v, st, bad)
+        s.set_state(U0)
+        s.step(2)
+        s.synchronize()
+        assert s.check_state() == (0, -1)
+        assert np.array_equal(s.get_state(), oracle.solve(md, o, U0, nsteps=2))

@@ -173,7 +173,10 @@ ma_status ma_host_initial_state(const ma_host_mesh* m, const ma_options* o, doub
  *      Cells.h:127) --------------------------------------------------------- */
 /* Uploads any mesh given as ma_mesh_view: builds the device face order, the
  * per-face Roe frame and the per-cell ordered contribution lists that replay
- * the reference's serial accumulation order. */
+ * the reference's serial accumulation order. At most MA_MAX_MESH_CELLS cells
+ * (the device arrays use 32-bit indices; MA_EINVAL beyond) and fewer than
+ * 2^30 faces. */
+#define MA_MAX_MESH_CELLS 143165576
 ma_status ma_mesh_upload(const ma_mesh_view* view, ma_mesh** out);
 /* As ma_mesh_upload; flags MA_MESH_CELL_FLUX also builds the per-cell lists
  * in element-local slot order (from every face set's flux_index) that

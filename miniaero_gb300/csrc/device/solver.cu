@@ -129,6 +129,10 @@ ma_status validate_view(const ma_mesh_view* v) {
   return MA_OK;
 }
 
+constexpr int32_t kMaxMeshCells = MA_MAX_MESH_CELLS;  // floor((2^31 - 1) / 15)
+static_assert(15LL * kMaxMeshCells <= 2147483647LL && 15LL * (kMaxMeshCells + 1) > 2147483647LL,
+              "the largest mesh whose gradient index fits int32");
+
 // Position of a BC type in the residual order Extrapolate, Tangent, NoSlip, Inflow.
 inline int type_rank(int type) {
   switch (type) {
@@ -149,6 +153,11 @@ extern "C" ma_status ma_mesh_upload_ex(const ma_mesh_view* v, int32_t flags, ma_
   const bool cell_flux = (flags & MA_MESH_CELL_FLUX) != 0;
   *out = nullptr;
   miniaero::TraceRange trace("ma_mesh_upload");
+  // Device arrays are indexed with 32-bit arithmetic; the widest per-cell
+  // array is the gradient, 15 values a cell at (3k + d) C + c.
+  if (v && v->ncells > kMaxMeshCells)
+    return set_error(MA_EINVAL, "mesh has " + std::to_string(v->ncells) + " cells; at most " +
+                                    std::to_string(kMaxMeshCells) + " fit the device's 32-bit indexing");
   ma_status st = validate_view(v);
   if (st != MA_OK) return st;
   try {

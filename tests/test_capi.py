@@ -1,4 +1,5 @@
 """C ABI: exported symbols, option parsing and error behaviour (CPU only)."""
+import ctypes
 import os
 import re
 import subprocess
@@ -116,6 +117,18 @@ def test_upload_rejects_bad_meshes():
     with pytest.raises(ma.MiniaeroError) as e:
         ma.DeviceMesh(md)
     assert e.value.status == _lib.MA_EINVAL
+
+
+def test_upload_rejects_meshes_beyond_32bit_indexing():
+    """The gradient arrays are indexed (3k + d) C + c in 32-bit arithmetic:
+    meshes above MA_MAX_MESH_CELLS are refused before any array is read."""
+    assert 15 * 143165576 <= 2 ** 31 - 1 < 15 * 143165577
+    view = _lib.ma_mesh_view()
+    view.ncells = 143165577
+    h = ctypes.c_void_p()
+    st = _lib.lib().ma_mesh_upload_ex(ctypes.byref(view), 0, ctypes.byref(h))
+    assert st == _lib.MA_EINVAL and not h
+    assert b"143165576" in _lib.lib().ma_last_error()
 
 
 def test_cli_reports_missing_input(tmp_path):

@@ -136,3 +136,40 @@ def test_cli_reports_missing_input(tmp_path):
     r = subprocess.run([b.CLI], cwd=tmp_path, capture_output=True, text=True)
     assert r.returncode != 0
     assert "does not exist" in r.stderr
+
+
+def declared_prototypes():
+    """{name: (return type text, [parameter texts])} from the header."""
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"#.*", "", text)
+    protos = {}
+    for m in re.finditer(r"([A-Za-z_][A-Za-z0-9_ \*]*?)\s*\b(ma_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", text, flags=re.S):
+        ret, name, params = m.group(1).strip(), m.group(2), " ".join(m.group(3).split())
+        args = [] if params in ("", "void") else [p.strip() for p in params.split(",")]
+        protos[name] = (ret, args)
+    return protos
+
+
+def test_ctypes_signatures_match_the_header():
+    """Every declared entry point has a ctypes signature with the header's
+    argument count, pointer parameters as pointers and the right return kind."""
+    protos = declared_prototypes()
+    assert set(protos) == set(declared_functions())
+    sigs = _lib._SIGNATURES
+    missing = sorted(set(protos) - set(sigs))
+    assert not missing, missing
+    for name, (ret, args) in protos.items():
+        res, argtypes = sigs[name]
+        assert len(argtypes) == len(args), (name, args, argtypes)
+        for text, t in zip(args, argtypes):
+            is_ptr = "*" in text
+            ctypes_ptr = t in (ctypes.c_void_p, ctypes.c_char_p) or (isinstance(t, type) and issubclass(
+                t, (ctypes._Pointer,)))
+            assert is_ptr == ctypes_ptr, (name, text, t)
+        if ret == "void":
+            assert res is None, name
+        elif "*" in ret:
+            assert res in (ctypes.c_void_p, ctypes.c_char_p), (name, ret, res)
+        else:
+            assert res is not None, name

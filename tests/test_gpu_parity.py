@@ -333,3 +333,43 @@ def test_state_check_reports_the_first_bad_cell(has_gpu):
         s.synchronize()
         assert s.check_state() == (0, -1)
         assert np.array_equal(s.get_state(), oracle.solve(md, o, U0, nsteps=2))
+
+
+def test_solvers_in_separate_threads_equal_sequential(has_gpu):
+    """Separate solvers driven from separate host threads (each capturing
+    and replaying its own step graph on its own stream) give the same bits as
+    the same solves run one after another."""
+    import threading
+    cases = []
+    for dims, prec in (((12, 6, 4), ma.MA_PREC_FP64), ((10, 8, 3), ma.MA_PREC_FP64), ((16, 4, 4), ma.MA_PREC_MIXED),
+                       ((9, 9, 2), ma.MA_PREC_MIXED)):
+        o = make_options(1, (1.0, 0.5, 0.25, 0.0), dims, 12, 2e-7, 1, 1, precision=prec)
+        md = ma.Parallel3DMesh.from_options(o).fill_mesh_data()
+        cases.append((md, o, ma.initial_state(md, o)))
+
+    def solve(md, o, U0):
+        with ma.TimeSolverExplicitRK4(md, o) as s:
+            s.set_state(U0)
+            for _ in range(3):
+                s.step(4)
+            s.synchronize()
+            return s.get_state()
+
+    expected = [solve(*c) for c in cases]
+    got = [None] * len(cases)
+    errors = []
+
+    def worker(i):
+        try:
+            got[i] = solve(*cases[i])
+        except Exception as e:  # reported below
+            errors.append(e)
+
+    threads = [threading.Thread(target=worker, args=(i,)) for i in range(len(cases))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join(timeout=300)
+    assert not errors, errors
+    for a, b in zip(got, expected):
+        assert_bitexact(a, b)

@@ -197,10 +197,148 @@ __device__ __forceinline__ void venkat_cell(const TopoView& t, const GeomView<do
   for (int k = 0; k < 5; ++k) phi[k * C + c] = (nm[k] == 1.0 && dm[k] == 1.0) ? 1.0 : nm[k] / dm[k];
 }
 
+// Warp buffer of the FP64 Venkatakrishnan limiter: one slot per (lane, face)
+// holding the face's selected stencil difference, du and |x_f - x_c|^2 (the
+// first two are overwritten by n and d), and the list of active slots.
+struct VenkatWarpBuf {
+  double a[32 * kMaxCellFaces];
+  double b[32 * kMaxCellFaces];
+  double e[32 * kMaxCellFaces];
+  uint8_t slot[32 * kMaxCellFaces];
+};
+constexpr int kVenkatBufBytes = static_cast<int>(sizeof(VenkatWarpBuf));
+
+__device__ __forceinline__ VenkatWarpBuf& venkat_warp_buf() {
+  extern __shared__ __align__(16) unsigned char venkat_smem[];
+  return reinterpret_cast<VenkatWarpBuf*>(venkat_smem)[threadIdx.x >> 5];
+}
+
+// Venkatakrishnan limiter of the warp's 32 cells in FP64. Every lane of the
+// warp calls it (a lane with !valid has no items and stores nothing).
+// phi = min(1, phi_f over the faces) with phi_f = RN(n_f / d_f); rounding is
+// monotone, so the minimum is RN(min_f n_f / d_f): the smallest ratio is
+// found with exact cross-multiplied comparisons and divided once per
+// component. Per component, each cell puts the faces whose du passes the
+// limiter's threshold in its buffer slots; then the warp either skips the
+// component (no such face), lets each lane evaluate its own slots (as many
+// rounds as its busiest lane has faces), or, when fewer rounds result, lists
+// the active slots end to end (prefix sum over the lanes) and has the 32
+// lanes evaluate the list 32 at a time, so a warp whose cells are partly
+// inside a wave does not run the formula on idle lanes. Each cell then
+// compares its own results in its face order, as the serial loop does, so
+// ties resolve identically and the bits are venkat_cell's. axis: the
+// cell's offsets lie along the axis of each face (slots 2p, 2p+1 normal to
+// axis p), so the dot products 0 + dx*gx + dy*gy + dz*gz reduce to their p
+// term (the others are signed zeros for finite gradients, which cannot change
+// a +0-started sum; a zero du is not limited either way).
+__device__ __forceinline__ void venkat_warp(const TopoView& t, const GeomView<double>& g, const double wc[5],
+                                            const double mn[5], const double mx[5], const double gsum[5][3],
+                                            double* __restrict__ phi, int c, bool valid, bool axis,
+                                            VenkatWarpBuf& buf) {
+  const int C = t.C, F = t.F;
+  const int lane = threadIdx.x & 31;
+  const int own = lane * kMaxCellFaces;
+  // |x_f - x_c|^2 per face, once per cell.
+  unsigned faces = 0;  // slots with a face
+#pragma unroll 1
+  for (int s = 0; s < kMaxCellFaces; ++s) {
+    const int code = t.csr_grad[s * C + c];
+    if (!valid || code < 0) continue;
+    faces |= 1u << s;
+    const int f = code >> 1;
+    const double* dv = (code & 1) ? g.dL : g.dR;
+    double dist;
+    if (axis) {
+      const double dp = dv[(s >> 1) * F + f];
+      dist = dp * dp;
+    } else {
+      dist = 0;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) dist += dv[d * F + f] * dv[d * F + f];
+    }
+    buf.e[own + s] = dist;
+  }
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const double dmax = mx[k] - wc[k], dmin = mn[k] - wc[k];  // the stencil differences
+    double gk[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) gk[d] = gsum[k][d];
+    unsigned act = 0;
+#pragma unroll 1
+    for (int s = 0; s < kMaxCellFaces; ++s) {
+      if (!((faces >> s) & 1u)) continue;
+      const int code = t.csr_grad[s * C + c];
+      const int f = code >> 1;
+      const double* dv = (code & 1) ? g.dL : g.dR;
+      double du;
+      if (axis) {
+        const int p = s >> 1;
+        du = dv[p * F + f] * (p == 0 ? gk[0] : p == 1 ? gk[1] : gk[2]);
+      } else {
+        du = 0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) du += dv[d * F + f] * gk[d];
+      }
+      // du > 1e-40 and du < -1e-40 as key comparisons (same result for non-NaN du).
+      const long long kd = okey(du);
+      const bool pos = kd > okey(1e-40), neg = kd < okey(-1e-40);
+      if (pos | neg) {
+        act |= 1u << s;
+        buf.a[own + s] = pos ? dmax : dmin;
+        buf.b[own + s] = du;
+      }
+    }
+    // Per warp: no item, each lane evaluating its own items (as many rounds
+    // as the busiest lane has items), or the compacted list (total / 32
+    // rounds plus the listing), whichever is shorter.
+    const unsigned cnt = __popc(act);
+    const unsigned most = __reduce_max_sync(0xffffffffu, cnt);
+    double nm = 1.0, dn = 1.0;
+    if (most) {
+      const unsigned total = __reduce_add_sync(0xffffffffu, cnt);
+      const bool compact = (total + 31) / 32 + 1 < most;
+      if (compact) {
+        unsigned incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += v;
+        }
+        unsigned at = incl - cnt;
+        for (unsigned m = act; m; m &= m - 1) buf.slot[at++] = static_cast<uint8_t>(own + __ffs(m) - 1);
+      }
+      __syncwarp();
+      auto evaluate = [&](int q) {
+        const double dm = buf.a[q], du = buf.b[q], eps2 = buf.e[q];
+        const bool neg = okey(du) < 0;  // du is past the threshold: its sign decides
+        buf.a[q] = negate_if((dm * dm + eps2) * du + 2 * du * du * dm, neg);
+        buf.b[q] = negate_if(du * (dm * dm + 2 * du * du + dm * du + eps2), neg);
+      };
+      if (compact) {
+        for (unsigned i = lane; i < total; i += 32) evaluate(buf.slot[i]);
+      } else {
+        for (unsigned m = act; m; m &= m - 1) evaluate(own + __ffs(m) - 1);
+      }
+      __syncwarp();
+      for (unsigned m = act; m; m &= m - 1) {
+        const int q = own + __ffs(m) - 1;
+        const double n = buf.a[q], d = buf.b[q];
+        if (ratio_less(n, d, nm, dn)) {
+          nm = n;
+          dn = d;
+        }
+      }
+      __syncwarp();  // the next component reuses the slots
+    }
+    if (valid) phi[k * C + c] = (nm == 1.0 && dn == 1.0) ? 1.0 : nm / dn;
+  }
+}
+
 // Limiter of one cell (MODE 1 Venkatakrishnan in FP32, MODE 2 Van Albada):
 // minimum over its faces of the limiter function, in serial face order.
 // AXIS: offsets along each face's axis only, slots grouped by axis as in
-// venkat_cell; du and |d|^2 reduce to their one nonzero term.
+// venkat_warp; du and |d|^2 reduce to their one nonzero term.
 template <class R, int MODE, bool AXIS>
 __device__ __forceinline__ void limiter_cell(const TopoView& t, const GeomView<R>& g, const R wc[5], const R mn[5],
                                              const R mx[5], const R gsum[5][3], R* __restrict__ phi, int c) {
@@ -336,9 +474,18 @@ __device__ __noinline__ void gradient_exact(const TopoView& t, const GeomView<do
 }
 
 // MODE: 0 gradient only (viscous first order), 1 + Venkatakrishnan, 2 + Van Albada.
-template <class R, int MODE>
+// WARP: the FP64 Venkatakrishnan limiter is evaluated across the warp
+// (venkat_warp; the batched sweep, whose small boxes leave many warps partly
+// inside a wave): all 32 lanes call the sweep, and a lane past the last cell
+// (valid false) recomputes a real cell and stores nothing. The single-mesh
+// sweep keeps the per-cell limiter (venkat_cell), faster where warps are
+// either wholly inside or wholly outside the waves. Both give the same bits.
+template <class R, int MODE, bool WARP>
+constexpr bool kWarpVenkat = WARP && MODE == 1 && std::is_same<R, double>::value;
+
+template <class R, int MODE, bool WARP = false>
 __device__ __forceinline__ void sweep1_cell(const TopoView& t, const GeomView<R>& g, const R* __restrict__ W,
-                                            R* __restrict__ grad, R* __restrict__ phi, int c) {
+                                            R* __restrict__ grad, R* __restrict__ phi, int c, bool valid = true) {
   const int C = t.C;
   R wc[5];
 #pragma unroll
@@ -359,6 +506,7 @@ __device__ __forceinline__ void sweep1_cell(const TopoView& t, const GeomView<R>
   bool exact_done = false;
   if constexpr (std::is_same<R, double>::value) {
     if (inexact) {  // rare: tiny quotients; redo the cell's sums with IEEE division
+      // (a lane with !valid recomputes a real cell: it writes that cell's own bits)
       gradient_exact(t, g, W, grad, c);
 #pragma unroll
       for (int k = 0; k < 5; ++k)
@@ -373,7 +521,7 @@ __device__ __forceinline__ void sweep1_cell(const TopoView& t, const GeomView<R>
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         gsum[k][d] = R(0) + acc[k][d];  // green_gauss_gradient_sum
-        grad[(3 * k + d) * C + c] = gsum[k][d];
+        if (valid) grad[(3 * k + d) * C + c] = gsum[k][d];
       }
   }
   if constexpr (MODE > 0) {
@@ -383,7 +531,9 @@ __device__ __forceinline__ void sweep1_cell(const TopoView& t, const GeomView<R>
       mn[k] = ex[k].min();
       mx[k] = ex[k].max();
     }
-    if constexpr (MODE == 1 && std::is_same<R, double>::value) {
+    if constexpr (kWarpVenkat<R, MODE, WARP>) {
+      venkat_warp(t, g, wc, mn, mx, gsum, phi, c, valid, (ac & 2) != 0, venkat_warp_buf());
+    } else if constexpr (MODE == 1 && std::is_same<R, double>::value) {
       if (ac & 2) venkat_cell<true>(t, g, wc, mn, mx, gsum, phi, c);
       else venkat_cell<false>(t, g, wc, mn, mx, gsum, phi, c);
     } else {
@@ -664,7 +814,11 @@ __global__ void __launch_bounds__(256, std::is_same<R, double>::value ? 2 : 0) k
     const int2 cs = chunks[ch];
     const Segment<R>& sg = segs[cs.x];
     const int c = cs.y + threadIdx.x;
-    if (c < sg.t.C) sweep1_cell<R, MODE>(sg.t, sg.g, sg.b.W, sg.b.grad, sg.b.phi, c);
+    if constexpr (kWarpVenkat<R, MODE, true>) {
+      sweep1_cell<R, MODE, true>(sg.t, sg.g, sg.b.W, sg.b.grad, sg.b.phi, c < sg.t.C ? c : sg.t.C - 1, c < sg.t.C);
+    } else if (c < sg.t.C) {
+      sweep1_cell<R, MODE>(sg.t, sg.g, sg.b.W, sg.b.grad, sg.b.phi, c);
+    }
   }
 }
 
@@ -777,7 +931,8 @@ cudaError_t launch_batch_stage_impl(const PathConfig& cfg, const Segment<R>* seg
     else if (cfg.limiter == 1)
       kb_sweep1<R, 2><<<g, b, 0, stream>>>(segs, bl.chunks[0], bl.nchunks + 0);
     else
-      kb_sweep1<R, 1><<<g, b, 0, stream>>>(segs, bl.chunks[0], bl.nchunks + 0);
+      kb_sweep1<R, 1><<<g, b, kWarpVenkat<R, 1, true> ? bl.block[0] / 32 * kVenkatBufBytes : 0, stream>>>(
+          segs, bl.chunks[0], bl.nchunks + 0);
   }
   if (kernels & kInternalFlux) {
     const dim3 g(bl.grid[1]), b(bl.block[1]);

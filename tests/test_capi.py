@@ -173,3 +173,18 @@ def test_ctypes_signatures_match_the_header():
             assert res in (ctypes.c_void_p, ctypes.c_char_p), (name, ret, res)
         else:
             assert res is not None, name
+
+
+def test_header_is_plain_c(tmp_path):
+    """The boundary is a C ABI: the header compiles as strict C99 and a C
+    program links against the library and calls it (no GPU needed)."""
+    from miniaero_gb300 import build as b
+    src = tmp_path / "main.c"
+    src.write_text('#include <stdio.h>\n#include "miniaero_gpu.h"\n'
+                   "int main(void) { ma_options o; ma_options_default(&o);\n"
+                   '  printf("%d %d %s\\n", ma_abi_version(), o.nx, ma_status_string(MA_EINVAL)); return 0; }\n')
+    exe = tmp_path / "main"
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.dirname(HEADER),
+                    str(src), "-L", b.BUILD, "-lminiaero_gpu", "-Wl,-rpath," + b.BUILD, "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    assert out[0] == "1" and out[1] == "10"

@@ -442,11 +442,16 @@ extern "C" ma_status ma_server_submit(ma_server* s, const ma_request* r, int64_t
   q.req = *r;
   q.key = key_of(*r);
   q.t_submit = ns_since(s->t0);
-  // A request that cannot fit even in an empty server is rejected now.
-  if (dry_member_bytes(s, *r) + dry_mesh_bytes(s, *r) > s->budget) {
+  // A request that can never run is rejected now: a mesh beyond the device
+  // arrays' 32-bit indexing (before any host mesh is built for it), or one
+  // that cannot fit even in an empty server.
+  int64_t cells, faces;
+  box_counts(*r, cells, faces);
+  const bool too_many = cells > MA_MAX_MESH_CELLS;
+  if (too_many || dry_member_bytes(s, *r) + dry_mesh_bytes(s, *r) > s->budget) {
     q.state = MA_REQ_FAILED;
-    q.error = MA_EBUDGET;
-    q.message = "request larger than the device-memory budget";
+    q.error = too_many ? MA_EINVAL : MA_EBUDGET;
+    q.message = too_many ? "request has more cells than MA_MAX_MESH_CELLS" : "request larger than the device-memory budget";
     q.t_finish = q.t_submit;
     s->stats.failed++;
   } else {

@@ -184,3 +184,18 @@ def test_launch_shapes_change_only_while_idle():
     assert s.query(rid).state == s.DONE
     s.set_launch([128] * 4, [1216] * 4)
     s.close()
+
+
+def test_request_beyond_the_index_limit_fails_at_submit():
+    """A box with more cells than the device arrays' 32-bit indexing allows
+    fails at once (MA_EINVAL), without building its mesh, even when the
+    budget would hold it."""
+    s = server(budget=1 << 50)
+    rid = s.submit(req(524))  # 524^3 = 143,877,824 cells > 143,165,576
+    info = s.query(rid)
+    assert info.state == s.FAILED and info.error == ma._lib.MA_EINVAL
+    ok = s.submit(req(16))
+    while s.poll():
+        pass
+    assert s.query(ok).state == s.DONE
+    s.close()

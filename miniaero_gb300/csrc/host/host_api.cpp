@@ -49,6 +49,12 @@ extern "C" ma_status ma_host_mesh_build(const ma_options* o, ma_host_mesh** out)
   if (!o || !out) return set_error(MA_EINVAL, "ma_host_mesh_build: null argument");
   *out = nullptr;
   miniaero::TraceRange trace("ma_host_mesh_build");
+  // The device arrays index a mesh with 32-bit arithmetic: refuse a box that
+  // ma_mesh_upload would refuse before building it.
+  if (o->nx > 0 && o->ny > 0 && o->nz > 0 &&
+      static_cast<int64_t>(o->nx) * o->ny * o->nz > MA_MAX_MESH_CELLS)
+    return set_error(MA_EINVAL, "ma_host_mesh_build: more than MA_MAX_MESH_CELLS (" +
+                                    std::to_string(MA_MAX_MESH_CELLS) + ") cells");
   miniaero::MeshSpec spec;
   spec.nx = o->nx; spec.ny = o->ny; spec.nz = o->nz;
   spec.lx = o->lx; spec.ly = o->ly; spec.lz = o->lz;

@@ -129,6 +129,10 @@ def test_upload_rejects_meshes_beyond_32bit_indexing():
     st = _lib.lib().ma_mesh_upload_ex(ctypes.byref(view), 0, ctypes.byref(h))
     assert st == _lib.MA_EINVAL and not h
     assert b"143165576" in _lib.lib().ma_last_error()
+    # The host mesh generator refuses such a box before building it.
+    with pytest.raises(ma.MiniaeroError) as e:
+        ma.Parallel3DMesh.from_options(ma.Options(nx=524, ny=524, nz=524)).fill_mesh_data()
+    assert e.value.status == _lib.MA_EINVAL
 
 
 def test_cli_reports_missing_input(tmp_path):

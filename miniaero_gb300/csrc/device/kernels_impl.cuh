@@ -33,6 +33,10 @@ constexpr int kFaceBlock = 128;
 // 128^3); the FP64 sweep is FP64-pipe bound at 2.
 template <class R>
 constexpr int kSweepMinBlocks = std::is_same<R, float>::value ? 5 : 2;
+// The FP32 face flux at 8 blocks of 128 (64 registers): 6 % faster than the
+// 7 blocks its approximate division and square root would otherwise leave.
+template <class R>
+constexpr int kFluxMinBlocks = std::is_same<R, float>::value ? 8 : 0;
 
 // Primitives of an FP64 state written as R: FP64 arithmetic for the plain
 // form (bit-exact), FP32 for the mixed form (its flux work is FP32 anyway).
@@ -779,7 +783,7 @@ __global__ void __launch_bounds__(kCellBlock, kSweepMinBlocks<R>) k_sweep1(TopoV
 }
 
 template <class R, bool SECOND, bool VISC>
-__global__ void __launch_bounds__(kFaceBlock) k_internal_flux(TopoView t, GeomView<R> g, const R* __restrict__ W,
+__global__ void __launch_bounds__(kFaceBlock, kFluxMinBlocks<R>) k_internal_flux(TopoView t, GeomView<R> g, const R* __restrict__ W,
                                                               const R* __restrict__ grad, const R* __restrict__ phi,
                                                               Transport tr, R* __restrict__ fflux) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;

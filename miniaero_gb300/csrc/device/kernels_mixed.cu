@@ -2,6 +2,7 @@
 // accumulation and RK4 update. Built with --fmad=false like the FP64 form:
 // without contraction every item's arithmetic is the same in the single-mesh
 // and the batched kernels, so a solve gives identical bits alone or batched.
+// FP32 division and square root are the approximate (2 ulp) forms.
 #include "kernels_impl.cuh"
 
 namespace miniaero {

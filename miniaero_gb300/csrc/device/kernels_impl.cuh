@@ -28,11 +28,12 @@ namespace {
 
 constexpr int kCellBlock = 256;
 constexpr int kFaceBlock = 128;
-// Resident sweep blocks per SM: the FP32 sweep waits on dependent gathers and
-// gains from 5 blocks (48 registers, a few bytes spilled: 9 % faster at
-// 128^3); the FP64 sweep is FP64-pipe bound at 2.
+// Resident sweep blocks per SM: the FP32 sweep waits on dependent gathers; at
+// 4 blocks (64 registers, no spill) it runs 12 % faster than at 5 (48
+// registers, 44 bytes spilled) with the approximate FP32 division. The FP64
+// sweep is FP64-pipe bound at 2.
 template <class R>
-constexpr int kSweepMinBlocks = std::is_same<R, float>::value ? 5 : 2;
+constexpr int kSweepMinBlocks = std::is_same<R, float>::value ? 4 : 2;
 // The FP32 face flux at 8 blocks of 128 (64 registers): 6 % faster than the
 // 7 blocks its approximate division and square root would otherwise leave.
 template <class R>

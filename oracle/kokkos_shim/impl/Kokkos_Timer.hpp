@@ -1,0 +1,2 @@
+// Kokkos::Impl::Timer lives in Kokkos_Core.hpp in this stand-in (see there).
+#include "../Kokkos_Core.hpp"

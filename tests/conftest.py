@@ -7,9 +7,6 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-REFERENCE = "/root/reference/kokkos"
-
-
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs on the GB300 box)")
     config.addinivalue_line("markers", "slow: longer CPU test")
@@ -41,9 +38,14 @@ def built():
 
 @pytest.fixture(scope="session")
 def reference_dir():
-    if not os.path.isdir(REFERENCE):
-        pytest.skip("reference tree not present on this machine")
-    return REFERENCE
+    """The reference's kokkos/ source tree: $MINIAERO_REFERENCE, else where the
+    oracle's reference-build recipe looks for it. Tests that read it skip where
+    it is absent (the GPU machine)."""
+    from oracle import build_ref
+    d = build_ref.reference_dir()
+    if d is None:
+        pytest.skip("reference tree not present (set MINIAERO_REFERENCE)")
+    return d
 
 
 @pytest.fixture(scope="session")

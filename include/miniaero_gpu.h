@@ -237,8 +237,13 @@ ma_status ma_solver_solve(ma_solver* s, const ma_host_mesh* host_mesh);
  * `stream` (a cudaStream_t, NULL = legacy default); returns after the stream
  * has reached the result. Scratch is a fixed 512 KiB array inside the
  * library; nothing is allocated. Meshes above 16,777,216 cells get MA_EINVAL.
- * The first call on a device sets up the scratch address (make it before any
- * stream capture). Calls that overlap on the GPU share the scratch and race. */
+ * The call runs on the mesh's device (the caller's current device is restored
+ * afterwards); d_state must be on that device. It synchronises `stream` to
+ * read dt back, so it must not be called on a stream that is being captured.
+ * The first call on a device sets up the scratch address and keeps it for the
+ * process (make that call before any global-mode capture on other streams; a
+ * cudaDeviceReset of the device invalidates it). Calls that overlap on the
+ * GPU share the scratch and race. */
 ma_status ma_cfl_dt_noalloc(const ma_mesh* mesh, const double* d_state, double cfl, double* dt_out, void* stream);
 
 /* ---- batched multi-mesh solver ------------------------------------------

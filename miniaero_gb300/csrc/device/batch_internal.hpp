@@ -13,6 +13,8 @@ dev::TopoView mesh_topo(const ma_mesh* m);
 // when the mesh was uploaded with MA_MESH_CELL_FLUX).
 dev::TopoView mesh_topo(const ma_mesh* m, int gather);
 bool mesh_has_cell_flux(const ma_mesh* m);
+// CUDA device index the mesh was uploaded to.
+int mesh_device(const ma_mesh* m);
 template <class R>
 dev::GeomView<R> mesh_geom(const ma_mesh* m);
 template <>

@@ -14,12 +14,18 @@
 // process exits). Meshes of up to kNoallocMaxBlocks * kCflBlock cells
 // (16,777,216) are accepted; larger ones get MA_EINVAL. Pass 1 writes the
 // partial of every block that pass 2 reads and pass 2 writes the result, so no
-// scratch entry has to start at zero. The first call on a device looks up the
+// scratch entry has to start at zero. Every call runs on the mesh's device
+// (made current for the call, the caller's current device restored after) and
+// d_state must live on that device. The first call on a device looks up the
 // array's device address (cudaGetSymbolAddress, which may load the module on
-// that device); make that first call before any stream capture begins. All
-// calls share the array: calls whose kernels overlap on the GPU (different
-// streams, or different host threads, without ordering between them) race on
-// it and may return each other's results.
+// that device) and keeps it for the life of the process, so a cudaDeviceReset
+// of that device (which unloads the module) invalidates the entry point on
+// it. The call reads dt back with a stream synchronisation: it cannot be made
+// on a stream that is being captured, and its first call on a device should
+// come before any capture in global mode on other streams. All calls share
+// the array: calls whose kernels overlap on the GPU (different streams, or
+// different host threads, without ordering between them) race on it and may
+// return each other's results.
 #include <cmath>
 #include <mutex>
 #include <string>
@@ -111,6 +117,27 @@ ma_status scratch_for_current_device(double** out) {
   return MA_OK;
 }
 
+// Makes a device current for one call and restores the caller's afterwards.
+class DeviceScope {
+ public:
+  explicit DeviceScope(int device) {
+    ok_ = cudaGetDevice(&previous_) == cudaSuccess;
+    if (ok_ && previous_ != device) {
+      ok_ = cudaSetDevice(device) == cudaSuccess;
+      switched_ = ok_;
+    }
+  }
+  ~DeviceScope() {
+    if (switched_) cudaSetDevice(previous_);
+  }
+  bool ok() const { return ok_; }
+
+ private:
+  int previous_ = 0;
+  bool ok_ = false;
+  bool switched_ = false;
+};
+
 }  // namespace
 
 extern "C" ma_status ma_cfl_dt_noalloc(const ma_mesh* mesh, const double* d_state, double cfl, double* dt_out,
@@ -123,6 +150,8 @@ extern "C" ma_status ma_cfl_dt_noalloc(const ma_mesh* mesh, const double* d_stat
   if (t.C > max_cells)
     return set_error(MA_EINVAL, "ma_cfl_dt_noalloc: mesh has " + std::to_string(t.C) +
                                     " cells; the allocation-free path accepts at most " + std::to_string(max_cells));
+  DeviceScope device(miniaero::mesh_device(mesh));
+  if (!device.ok()) return set_error(MA_ECUDA, "ma_cfl_dt_noalloc: cannot make the mesh's device current");
   double* scratch = nullptr;
   ma_status st = scratch_for_current_device(&scratch);
   if (st != MA_OK) return st;

@@ -536,6 +536,7 @@ dev::TopoView mesh_topo(const ma_mesh* m, int gather) {
   return gather == MA_GATHER_CELL_FLUX ? m->topo_cf : m->topo;
 }
 bool mesh_has_cell_flux(const ma_mesh* m) { return m->has_cell_flux; }
+int mesh_device(const ma_mesh* m) { return m->device; }
 template <>
 dev::GeomView<double> mesh_geom<double>(const ma_mesh* m) { return m->g64; }
 template <>

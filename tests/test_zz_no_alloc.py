@@ -2,7 +2,8 @@
 solver's own CFL evaluation (ma_solver_set_state, which reduces in its arena):
 the same dt bit for bit on consecutive calls, across meshes whose block counts
 differ (a call runs over partial minima the previous call left behind), at the
-largest accepted mesh, and a clear error one cell beyond it. The file name
+largest accepted mesh, and a clear error one cell beyond it; repeated calls
+leave the device's free memory unchanged. The file name
 sorts last so that the suite also runs it after every other GPU test."""
 import copy
 import ctypes
@@ -81,6 +82,35 @@ def uniform_state(ncells):
     U[:, 3] = 0.0
     U[:, 4] = 1e5 / 0.4 + 0.5 * 1.2 * (100.0 ** 2 + 30.0 ** 2)
     return U
+
+
+@pytest.mark.gpu
+def test_calls_leave_device_memory_unchanged(has_gpu):
+    """The property the entry point exists for: after a first call (which may
+    load the module on the device), further calls on the largest accepted mesh
+    change the device's free memory by nothing."""
+    import torch
+    o = ma.Options(problem_type=1, nx=4, ny=4, nz=2, ntimesteps=1, cfl=0.5)
+    template = ma.Parallel3DMesh.from_options(o).fill_mesh_data()
+    md = faceless_mesh(MAX_CELLS, template)
+    dm = ma.DeviceMesh(md)
+    U = uniform_state(MAX_CELLS)
+    d = torch.from_numpy(np.ascontiguousarray(U.T)).to("cuda")
+    torch.cuda.synchronize()
+    dt = ctypes.c_double(0.0)
+
+    def call():
+        check(lib().ma_cfl_dt_noalloc(dm._h, ctypes.c_void_p(d.data_ptr()), 0.5, ctypes.byref(dt), None))
+        return dt.value
+
+    first = call()
+    free_before, _ = torch.cuda.mem_get_info()
+    values = [call() for _ in range(10)]
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before
+    assert values == [first] * 10 and np.isfinite(first) and first > 0.0
+    del d
+    dm.close()
 
 
 @pytest.mark.gpu

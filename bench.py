@@ -1,26 +1,38 @@
 """Benchmark of the RK4 residual path on one GB300 (or N replicas).
 
-Workload (default, N=1): Sod shock tube at scale, 256x128x128 Hexa8 cells
-(4,194,304) on 1.0x0.5x0.5, rho/p = 1/1 | 0.125/0.1, second order with
-Green-Gauss gradients and the Venkatakrishnan limiter, viscous (constant
-mu = 1.8e-5, Pr = 0.72), dt from CFL 0.5 at t = 0, plain FP64. A "step" is one
-RK4 time step (4 stages) over the whole mesh; the unit of work is one
-cell-stage, metric Mcell-stage/s = cells * 4 * steps / seconds / 1e6.
+Default run (N=1): three configurations, each measured end to end.
+  * Headline: Sod shock tube at scale, 256x128x128 Hexa8 cells (4,194,304)
+    on 1.0x0.5x0.5, rho/p = 1/1 | 0.125/0.1, second order with Green-Gauss
+    gradients and the Venkatakrishnan limiter, viscous (constant mu = 1.8e-5,
+    Pr = 0.72), dt from CFL 0.5 at t = 0, plain FP64; K timed steps.
+  * The first-order inviscid Sod tube on 128x16x16 (dt 1e-5) and the viscous
+    flat plate on 512x128x128 (Mach 0.3, Van Albada), each timed over its
+    configured step count (200 and 50).
+A "step" is one RK4 time step (4 stages) over the whole mesh; the unit of
+work is one cell-stage, metric Mcell-stage/s = cells * 4 * steps / s / 1e6.
 
-Timing: W warm-up steps, then K steps as CUDA graph launches bracketed by a
-barrier and device synchronisation, timed with CUDA events on the solver's
-stream. Working set (state, gradients, face data) is ~3 GB, far above the
-129 MB L2. The mixed form (FP32 flux/gradient/limiter, FP64 accumulation and
-RK update) is measured on the same mesh and reported with its error against
-the FP64 result. The end-to-end figure times, per step, the host->device copy
-of the state from pinned memory, the step and the device->host copy of the
-result, all through the C ABI.
+Timing: W warm-up steps, then the timed steps as CUDA graph launches
+bracketed by a barrier and device synchronisation, timed with CUDA events on
+the solver's stream. The large meshes' working sets (3-7 GB) are far above
+the 129 MB L2; the 32,768-cell mesh fits in L2 and runs back to back as a
+solve does. The mixed form (FP32 flux/gradient/limiter, FP64 accumulation and
+RK update) is timed on the same meshes, its error against FP64 taken after
+each configuration's own step count (200 / 100 / 50). The end-to-end figure
+times, per step, the host->device copy of the state from pinned memory, the
+step and the device->host copy of the result, all through the C ABI. The CPU
+baseline is the oracle port on all host threads, built as the reference's
+Makefile builds (-O3, default contraction; the -O2 no-contraction parity
+build is timed beside it on the headline). Then the batched ensemble and the
+serving loop (saturating stream and 25/50/90 % offered loads). The JSON
+line ends with a compact summary of every configuration.
 
 --impl reference times the CPU restatement of the reference's Kokkos OpenMP
-loops (oracle port, all host threads) on the same workload.
+loops (oracle port, -O3 timing build, all host threads) on the headline
+configuration, with the same config dict.
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -156,6 +168,9 @@ def kernel_rooflines(md, prof, w, sm_mhz, fp64_rates=None, counted=True, second_
                 "peak_source": peak_kind, "unit": "GB/s", "frac": d["achieved_GBps"] / peak,
                 "traffic": (load_traffic(traffic_key) or {}).get(dom) if traffic_key else None,
                 "algorithmic_bytes_per_launch": d["algorithmic_bytes"], "ms_per_launch": d["ms_per_launch"]}
+    if roofline["traffic"] is not None:
+        roofline["traffic_scaled_from"] = ("128^3 ncu capture (sod_2nd_viscous_128x128x128), scaled by the items "
+                                           "per launch; profiles/ncu_traffic.json")
     if "fp64_pipe_frac" in d:
         roofline["fp64_pipe"] = {"frac": d["fp64_pipe_frac"], "peak_inst_per_s": fp64_peak,
                                  "note": "FP64 thread instructions per item from the ncu summary; the plain form "
@@ -287,10 +302,243 @@ def allreduce_max(world, value):
     return float(t.item())
 
 
-def cpu_baseline_sample(ma, oracle, md, o, U0, dt, seconds=15.0, nthreads=None):
-    """Times the oracle port (OpenMP, all host threads) on whole-mesh steps."""
+# The configurations the default run measures: (workload, RK4 steps the
+# configuration specifies; the mixed form's error is taken after that many
+# steps). The Sod 256x128x128 mesh is the headline (value, e2e, roofline).
+CONFIG_SUITE = [("sod_1st_inviscid_128x16x16", 200), ("sod_2nd_viscous_256x128x128", 100),
+                ("flat_plate_vanalbada_512x128x128", 50)]
+DATA_NOTE = "synthetic (seeded mesh generator; analytic Sod / flat-plate initial states)"
+
+
+def rel_errors(Um, U):
+    """Relative L2 error per conserved variable, momentum components against
+    the momentum norm (a component that is zero in exact arithmetic, like the
+    transverse momentum of Sod, has no meaningful relative error)."""
+    mom = max(float(np.linalg.norm(U[:, 1:4])), 1e-300)
+    return [float(np.linalg.norm(Um[:, k] - U[:, k]) / (mom if k in (1, 2, 3) else
+                                                         max(np.linalg.norm(U[:, k]), 1e-300))) for k in range(5)]
+
+
+def measure_config(ma, args, world, rank, local, name, err_steps, timed_steps, cpu=("timing",), cpu_seconds=10.0):
+    """One configuration end to end: FP64 throughput device-resident and
+    through the C ABI with host copies, per-kernel rooflines, the mixed form's
+    throughput and its error after the configured steps, and the CPU
+    baseline(s) on rank 0."""
+    import torch
+    o = make_options(ma, name, "fp64")
+    md = ma.Parallel3DMesh.from_options(o).fill_mesh_data()
+    U0 = ma.initial_state(md, o)
+    C = md.ncells
+    dmesh = ma.DeviceMesh(md)
+    solver = ma.TimeSolverExplicitRK4(md, o, device_mesh=dmesh)
+    solver.set_state(U0)
+    dt = solver.dt
+    solver.step(args.warmup)
+    solver.synchronize()
+    U_start = solver.get_state()  # state entering the timed region (AOS)
+
+    # ---- timed region: K steps from device-resident state ----
+    sampler = ClockSampler(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    sampler.start()
+    ms = time_steps(ma, solver, timed_steps)
+    clocks = sampler.stop()
+    barrier(world)
+    ms = allreduce_max(world, ms)
+    launches = solver.launches_per_step * timed_steps
+    value = world * C * 4 * timed_steps / (ms / 1e3) / 1e6
+
+    # ---- per-kernel durations (same workload, kernels launched one by one) ----
+    prof = solver.profile_steps(max(2, min(timed_steps, 10)))
+    fp64_rates = {op: ma.fp64_rate(op) for op in ("add", "mul", "fma")}
+    wl = WORKLOADS[name]
+    second_viscous = bool(wl.get("second_order_space") and wl.get("viscous"))
+    # The ncu per-item FP64 counts were captured on the Sod second-order
+    # viscous workloads; the traffic table is scaled to the 256x128x128 mesh.
+    counted = name.startswith("sod_2nd_viscous")
+    scaled = name == DEFAULT_WORKLOAD
+    roofline, kernels = kernel_rooflines(md, prof, 8, clocks.get("sm_mhz"), fp64_rates, counted, second_viscous,
+                                         "traffic_bytes_per_launch" if scaled else None)
+    roofline["stage"] = stage_roofline(C, prof, 8) if second_viscous else None
+
+    # ---- FP64 and mixed after the configured step count, from the initial state ----
+    solver.set_state(U0)
+    solver.dt = dt
+    solver.step(err_steps)
+    solver.synchronize()
+    U_fp64 = solver.get_state()
+    om = make_options(ma, name, "mixed")
+    msolver = ma.TimeSolverExplicitRK4(md, om, device_mesh=dmesh)
+    msolver.set_state(U0)
+    msolver.dt = dt
+    msolver.step(err_steps)
+    msolver.synchronize()
+    errs = rel_errors(msolver.get_state(), U_fp64)
+    msolver.set_state(U_start)
+    msolver.dt = dt
+    msolver.step(args.warmup)
+    msolver.synchronize()
+    mms = allreduce_max(world, time_steps(ma, msolver, timed_steps))
+    mvalue = world * C * 4 * timed_steps / (mms / 1e3) / 1e6
+    mprof = msolver.profile_steps(2)
+    mroofline, mkernels = kernel_rooflines(md, mprof, 4, clocks.get("sm_mhz"), None, counted, second_viscous,
+                                           "traffic_bytes_per_launch_mixed" if scaled else None)
+    mroofline["stage"] = stage_roofline(C, mprof, 4) if second_viscous else None
+    msolver.close()
+
+    # ---- end to end through the C ABI with pinned host buffers ----
+    eo = make_options(ma, name, "fp64")
+    eo.cfl = 0.0
+    eo.dt = dt
+    esolver = ma.TimeSolverExplicitRK4(md, eo, device_mesh=dmesh)
+    # Component-major host buffers (MA_LAYOUT_SOA): each step uploads the
+    # state that entered the timed region above and reads back its successor.
+    hU = torch.empty((5, C), dtype=torch.float64).pin_memory()
+    hU.numpy()[:] = U_start.T
+    hOut = torch.empty((5, C), dtype=torch.float64).pin_memory()
+    state_bytes = C * 5 * 8
+    L = ma._lib.lib()
+    inp = ma._lib.f64p(hU.numpy())
+    outp = ma._lib.f64p(hOut.numpy())
+
+    def e2e_step():
+        ma._lib.check(L.ma_solver_set_state(esolver._h, inp, ma.MA_LAYOUT_SOA))
+        ma._lib.check(L.ma_solver_step(esolver._h, 1))
+        ma._lib.check(L.ma_solver_get_state(esolver._h, outp, ma.MA_LAYOUT_SOA))
+
+    for _ in range(max(1, min(args.warmup, 2))):
+        e2e_step()
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(timed_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = allreduce_max(world, time.perf_counter() - t0)
+    barrier(world)
+    e2e_value = world * C * 4 * timed_steps / e2e_s / 1e6
+    # The SoA round trip must give the bits of the same step through the AOS path.
+    esolver.set_state(U_start)
+    esolver.step(1)
+    e2e_verified = bool(np.array_equal(esolver.get_state(), hOut.numpy().T))
+    esolver.close()
+    solver.close()
+
+    cpu_results = {}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import oracle
+        for build in cpu:
+            cpu_results[build] = cpu_baseline_sample(ma, oracle, md, o, U0, dt, seconds=cpu_seconds,
+                                                     timing=(build == "timing"))
+    dmesh.close()
+    res = {
+        "config": config_dict(name, md, o, world), "dt": dt, "timed_steps": timed_steps,
+        "value": value, "ms_per_step": ms / timed_steps, "clocks": clocks, "gpu_launches": launches,
+        "e2e": {"value": e2e_value, "unit": "Mcell-stage/s", "h2d_bytes_per_step": state_bytes,
+                "d2h_bytes_per_step": state_bytes,
+                "path": "ma_solver_set_state + ma_solver_step + ma_solver_get_state, pinned host SoA buffers",
+                "input": "state after the warm-up steps", "verified_vs_aos_path": e2e_verified},
+        "roofline": roofline, "kernels": kernels,
+        "mixed": {"value": mvalue, "unit": "Mcell-stage/s", "ms_per_step": mms / timed_steps,
+                  "speedup_vs_fp64": mvalue / value, "rel_l2_error_vs_fp64": errs,
+                  "error_note": "momentum components relative to the momentum norm",
+                  "error_after_steps": err_steps, "roofline": mroofline, "kernels": mkernels},
+        "cpu_baseline": cpu_results.get("timing"),
+    }
+    if "parity" in cpu_results:
+        res["cpu_baseline_parity_build"] = cpu_results["parity"]
+    return res
+
+
+def _r(x, n=4):
+    """Rounds to n significant digits for the compact summary."""
+    if x is None or not isinstance(x, float) or x == 0.0 or not math.isfinite(x):
+        return x
+    return float("%.*g" % (n, x))
+
+
+def compact(name, r):
+    """A few numbers per configuration for the end of the JSON line."""
+    cpu = r.get("cpu_baseline") or {}
+    st = (r["roofline"].get("stage") or {})
+    mst = (r["mixed"]["roofline"].get("stage") or {})
+    out = {"cells": r["config"]["cells"], "timed_steps": r["timed_steps"], "fp64": _r(r["value"]),
+           "e2e": _r(r["e2e"]["value"]), "cpu": _r(cpu.get("value")),
+           "e2e_vs_cpu": _r(r["e2e"]["value"] / cpu["value"]) if cpu.get("value") else None,
+           "mixed": _r(r["mixed"]["value"]), "mixed_speedup": _r(r["mixed"]["speedup_vs_fp64"]),
+           "mixed_err": [_r(e, 2) for e in r["mixed"]["rel_l2_error_vs_fp64"]],
+           "err_steps": r["mixed"]["error_after_steps"]}
+    if st:
+        out["stage_hbm_frac"] = _r(st["frac"], 3)
+    if mst:
+        out["mixed_stage_hbm_frac"] = _r(mst["frac"], 3)
+    return out
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    import miniaero_gb300 as ma
+    torch.cuda.set_device(local)
+    suite = [(n, s) for n, s in CONFIG_SUITE if args.workload == "all" or n == args.workload]
+    if args.workload not in ("all",) and not suite:
+        suite = [(args.workload, WORKLOADS[args.workload].get("ntimesteps", 100))]
+    headline = DEFAULT_WORKLOAD if any(n == DEFAULT_WORKLOAD for n, _ in suite) else suite[0][0]
+    results = {}
+    for name, err_steps in suite:
+        if name == headline:
+            timed, cpu = args.steps, ("timing", "parity")
+        else:
+            # Secondary configurations: their own step counts are timed (the
+            # small mesh takes 200 steps of ~0.4 ms; the 8.4 M-cell flat plate 50).
+            timed, cpu = max(args.steps, err_steps), ("timing",)
+        results[name] = measure_config(ma, args, world, rank, local, name, err_steps, timed, cpu,
+                                       cpu_seconds=(12.0 if name == headline else 8.0))
+
+    batched = serving = None
+    if not args.no_extras:
+        batched = run_batched(ma, steps=max(2, min(args.steps, 10)), warmup=args.warmup)
+        serving = run_serving_suite(ma, n_requests=args.serve_requests)
+
+    if rank == 0:
+        h = results[headline]
+        line = {
+            "metric": "Mcell-stage/s", "value": h["value"], "unit": "Mcell-stage/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": h["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": DATA_NOTE, "config": h["config"], "clocks": h["clocks"], "e2e": h["e2e"],
+            "gpu_launches": h["gpu_launches"], "roofline": h["roofline"], "cpu_baseline": h["cpu_baseline"],
+            "cpu_baseline_parity_build": h.get("cpu_baseline_parity_build"),
+            "kernels": h["kernels"], "mixed": h["mixed"],
+            "other_configs": {n: {k: v for k, v in r.items() if k not in ("kernels",)}
+                              for n, r in results.items() if n != headline},
+            "batched": batched,
+            "serving": serving,
+        }
+        # Last, so that a reader of only the end of the output sees them: the
+        # key numbers of every configuration, the batch and the serving loads.
+        summary = {n: compact(n, r) for n, r in results.items()}
+        if batched:
+            summary["batched_64_sod_boxes"] = {"fp64": _r(batched["fp64"]["value"]),
+                                               "mixed": _r(batched["mixed"]["value"])}
+        if serving:
+            summary["serving"] = serving["summary"]
+        line["summary"] = summary
+        print(json.dumps(line), flush=True)
+
+
+ORACLE_BUILDS = {
+    True: "oracle port at -O3 with the compiler's default multiply-add contraction (the reference Makefile's "
+          "flags, kokkos/Makefile:17)",
+    False: "oracle port at -O2 -ffp-contract=off (the parity build)",
+}
+
+
+def cpu_baseline_sample(ma, oracle, md, o, U0, dt, seconds=15.0, nthreads=None, timing=True):
+    """Times the oracle port (OpenMP, all host threads) on whole-mesh steps.
+    timing=True uses its -O3 timing build, False the parity build."""
     nthreads = nthreads or os.cpu_count() or 1
-    st = oracle.Stepper(md, o, U0, dt=dt, nthreads=nthreads)
+    st = oracle.Stepper(md, o, U0, dt=dt, nthreads=nthreads, timing=timing)
     t0 = time.perf_counter()
     st.step(1)
     per_step = time.perf_counter() - t0
@@ -310,8 +558,27 @@ def cpu_baseline_sample(ma, oracle, md, o, U0, dt, seconds=15.0, nthreads=None):
     st.close()
     value = md.ncells * 4 * nsteps / elapsed / 1e6
     return {"value": value, "unit": "Mcell-stage/s", "cores": nthreads, "kind": "port",
+            "build": ORACLE_BUILDS[bool(timing)],
             "sample": "%d RK4 steps of the full %d-cell mesh after %d untimed step%s (%.1f s)"
                       % (nsteps, md.ncells, untimed, "" if untimed == 1 else "s", elapsed)}
+
+
+def config_dict(name, md, o, world):
+    """The workload as both arms report it (identical keys and values)."""
+    wl = WORKLOADS[name]
+    cfg = {"workload": name, "cells": md.ncells, "internal_faces": md.internal.nfaces, "precision": "fp64"}
+    if wl.get("cfl"):
+        cfg["cfl"] = wl["cfl"]
+    else:
+        cfg["dt"] = wl["dt"]
+    state_mb = md.ncells * 0.8e-3  # ~0.8 KB of device arrays per cell in the FP64 form
+    if state_mb > 1000.0:
+        cfg["l2"] = "working set ~%.0f GB >> 129 MB L2 (no flush needed)" % (state_mb / 1e3)
+    else:
+        cfg["l2"] = ("working set ~%.0f MB fits the 129 MB L2; steps run back to back as a solve does (no flush)"
+                     % state_mb)
+    cfg["parallelism"] = "replicas" if world > 1 else "single GPU"
+    return cfg
 
 
 def run_reference(args, world, rank):
@@ -327,7 +594,7 @@ def run_reference(args, world, rank):
     if o.cfl > 0:
         dt = cfl_dt_host(md, U0, o.cfl)
     nthreads = os.cpu_count() or 1
-    st = oracle.Stepper(md, o, U0, dt=dt, nthreads=nthreads)
+    st = oracle.Stepper(md, o, U0, dt=dt, nthreads=nthreads, timing=True)
     tw = time.perf_counter()
     st.step(args.warmup)
     per_step = (time.perf_counter() - tw) / max(args.warmup, 1)
@@ -345,10 +612,10 @@ def run_reference(args, world, rank):
     line = {
         "impl": "reference", "metric": "Mcell-stage/s", "value": value, "unit": "Mcell-stage/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / timed * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": name, "cells": md.ncells, "precision": "fp64", "dt": dt},
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": DATA_NOTE, "config": config_dict(name, md, o, world),
         "cpu_baseline": {"value": value, "unit": "Mcell-stage/s", "cores": nthreads, "kind": "port",
-                         "sample": sample},
+                         "build": ORACLE_BUILDS[True], "sample": sample},
         "e2e": {"value": value, "unit": "Mcell-stage/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -388,160 +655,6 @@ def time_steps(ma, solver, K):
     solver.synchronize()
     torch.cuda.synchronize()
     return e0.elapsed_time(e1)
-
-
-def run_ours(args, world, rank, local):
-    import torch
-    import miniaero_gb300 as ma
-    torch.cuda.set_device(local)
-    name = args.workload
-    o = make_options(ma, name, "fp64")
-    md = ma.Parallel3DMesh.from_options(o).fill_mesh_data()
-    U0 = ma.initial_state(md, o)
-    C = md.ncells
-    dmesh = ma.DeviceMesh(md)
-    solver = ma.TimeSolverExplicitRK4(md, o, device_mesh=dmesh)
-    solver.set_state(U0)
-    dt = solver.dt
-    solver.step(args.warmup)
-    solver.synchronize()
-    U_start = solver.get_state()  # state entering the timed region (AOS)
-
-    # ---- timed region: K steps from device-resident state ----
-    sampler = ClockSampler(local)
-    barrier(world)
-    torch.cuda.synchronize()
-    sampler.start()
-    ms = time_steps(ma, solver, args.steps)
-    clocks = sampler.stop()
-    barrier(world)
-    ms = allreduce_max(world, ms)
-    launches = solver.launches_per_step * args.steps
-    value = world * C * 4 * args.steps / (ms / 1e3) / 1e6
-    U_fp64 = solver.get_state()
-    steps_fp64 = solver.steps_done
-
-    # ---- per-kernel durations (same workload, kernels launched one by one) ----
-    prof = solver.profile_steps(max(2, min(args.steps, 10)))
-    Fi = md.internal.nfaces
-    fp64_rates = {op: ma.fp64_rate(op) for op in ("add", "mul", "fma")}
-    # The ncu per-item FP64 counts and the two-sweep stage model are for the
-    # second-order viscous path; the counts were captured on the Sod workloads.
-    wl = WORKLOADS[name]
-    second_viscous = bool(wl.get("second_order_space") and wl.get("viscous"))
-    counted = name.startswith("sod_2nd_viscous")
-    scaled = name == DEFAULT_WORKLOAD  # the ncu traffic tables are scaled to this workload's launches
-    roofline, kernels = kernel_rooflines(md, prof, 8, clocks.get("sm_mhz"), fp64_rates, counted, second_viscous,
-                                         "traffic_bytes_per_launch" if scaled else None)
-    roofline["stage"] = stage_roofline(C, prof, 8) if second_viscous else None
-
-    # ---- mixed form on the same mesh: throughput and error vs FP64 ----
-    om = make_options(ma, name, "mixed")
-    msolver = ma.TimeSolverExplicitRK4(md, om, device_mesh=dmesh)
-    msolver.set_state(U0)
-    msolver.dt = dt
-    msolver.step(args.warmup)
-    msolver.synchronize()
-    mms = time_steps(ma, msolver, args.steps)
-    mms = allreduce_max(world, mms)
-    mvalue = world * C * 4 * args.steps / (mms / 1e3) / 1e6
-    msolver.set_state(U0)
-    msolver.dt = dt
-    msolver.step(steps_fp64)
-    msolver.synchronize()
-    Um = msolver.get_state()
-    errs = [float(np.linalg.norm(Um[:, k] - U_fp64[:, k]) / max(np.linalg.norm(U_fp64[:, k]), 1e-300))
-            for k in range(5)]
-    # Momentum components whose FP64 values are near zero (transverse momentum
-    # in Sod) give large ratios above; these scale by the momentum magnitude.
-    mom = max(float(np.linalg.norm(U_fp64[:, 1:4])), 1e-300)
-    errs_mom = [float(np.linalg.norm(Um[:, k] - U_fp64[:, k]) / mom) for k in (1, 2, 3)]
-    mprof = msolver.profile_steps(2)
-    # FP32 work arrays: algorithmic bytes at 4 bytes per value, against HBM.
-    mroofline, mkernels = kernel_rooflines(md, mprof, 4, clocks.get("sm_mhz"), None, counted, second_viscous)
-    mroofline["traffic"] = ((load_traffic("traffic_bytes_per_launch_mixed") or {}).get(mroofline["kernel"])
-                            if scaled else None)
-    mroofline["stage"] = stage_roofline(C, mprof, 4) if second_viscous else None
-    msolver.close()
-
-    # ---- end to end through the C ABI with pinned host buffers ----
-    eo = make_options(ma, name, "fp64")
-    eo.cfl = 0.0
-    eo.dt = dt
-    esolver = ma.TimeSolverExplicitRK4(md, eo, device_mesh=dmesh)
-    # Component-major host buffers (MA_LAYOUT_SOA): each step uploads the
-    # state that entered the timed region above and reads back its successor.
-    hU = torch.empty((5, C), dtype=torch.float64).pin_memory()
-    hU.numpy()[:] = U_start.T
-    hOut = torch.empty((5, C), dtype=torch.float64).pin_memory()
-    state_bytes = C * 5 * 8
-    L = ma._lib.lib()
-    inp = ma._lib.f64p(hU.numpy())
-    outp = ma._lib.f64p(hOut.numpy())
-
-    def e2e_step():
-        ma._lib.check(L.ma_solver_set_state(esolver._h, inp, ma.MA_LAYOUT_SOA))
-        ma._lib.check(L.ma_solver_step(esolver._h, 1))
-        ma._lib.check(L.ma_solver_get_state(esolver._h, outp, ma.MA_LAYOUT_SOA))
-
-    for _ in range(max(1, min(args.warmup, 2))):
-        e2e_step()
-    barrier(world)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        e2e_step()
-    torch.cuda.synchronize()
-    e2e_s = allreduce_max(world, time.perf_counter() - t0)
-    barrier(world)
-    e2e_value = world * C * 4 * args.steps / e2e_s / 1e6
-    # The SoA round trip must give the bits of the same step through the AOS path.
-    esolver.set_state(U_start)
-    esolver.step(1)
-    e2e_verified = bool(np.array_equal(esolver.get_state(), hOut.numpy().T))
-    esolver.close()
-
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        import oracle
-        cpu = cpu_baseline_sample(ma, oracle, md, o, U0, dt)
-    solver.close()
-    esolver = None
-    dmesh.close()
-    del md
-
-    batched = serving = None
-    if not args.no_extras:
-        batched = run_batched(ma, steps=max(2, min(args.steps, 10)), warmup=args.warmup)
-        serving = run_serving(ma, n_requests=args.serve_requests)
-
-    if rank == 0:
-        line = {
-            "metric": "Mcell-stage/s", "value": value, "unit": "Mcell-stage/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded mesh generator; Sod initial state)",
-            "config": {"workload": name, "cells": C, "internal_faces": Fi, "precision": "fp64", "dt": dt,
-                       "l2": "working set ~3 GB >> 129 MB L2 (no flush needed)",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
-            "clocks": clocks,
-            "e2e": {"value": e2e_value, "unit": "Mcell-stage/s", "h2d_bytes_per_step": state_bytes,
-                    "d2h_bytes_per_step": state_bytes,
-                    "path": "ma_solver_set_state + ma_solver_step + ma_solver_get_state, pinned host SoA buffers",
-                    "input": "state after the warm-up steps", "verified_vs_aos_path": e2e_verified},
-            "gpu_launches": launches,
-            "roofline": roofline,
-            "kernels": kernels,
-            "mixed": {"value": mvalue, "unit": "Mcell-stage/s", "ms_per_step": mms / args.steps,
-                      "speedup_vs_fp64": mvalue / value, "rel_l2_error_vs_fp64": errs,
-                      "momentum_error_vs_fp64_momentum_norm": errs_mom,
-                      "error_after_steps": int(steps_fp64),
-                      "roofline": mroofline, "kernels": mkernels},
-            "cpu_baseline": cpu,
-            "batched": batched,
-            "serving": serving,
-        }
-        print(json.dumps(line), flush=True)
 
 
 def ensemble_members(ma, n=64, seed=0, lo=16, hi=96):
@@ -623,28 +736,40 @@ def run_batched(ma, steps, warmup, n_members=64):
     return res
 
 
-def run_serving(ma, n_requests=32, rate=200.0, nsteps=500, seed=1, budget=150 << 30, tick=25,
-                max_running_cells=8_000_000):
-    """Serving stream: Poisson arrivals (rate/s, seeded) of flat-plate solves,
-    Mach uniform in [0.1, 0.6], sizes from {32,48,64,96,128}^3, nsteps RK4
-    steps each, mixed precision, admitted under the HBM budget with at most
-    max_running_cells cells running at once (enough to fill the GPU). The
-    server runs its batch with the launch shapes the autotuner picked for the
-    same requests as one static batch (tuned once for the workload, before
-    the stream starts)."""
+SERVE_SIZES = [32, 48, 64, 96, 128]
+SERVE_STEPS = 500
+
+
+def serving_requests(ma, n_requests, rate, seed=1):
+    """The serving stream's requests: Poisson arrivals at `rate` per second
+    (seeded), flat-plate solves with Mach uniform in [0.1, 0.6] on n^3 meshes,
+    n uniform from SERVE_SIZES. The same seed gives the same request mix at
+    every rate; only the arrival times scale."""
     rng = np.random.default_rng(seed)
-    sizes = [32, 48, 64, 96, 128]
-    phys = ma.Options(problem_type=1, second_order_space=1, viscous=1, limiter=ma.MA_LIMITER_VANALBADA,
+    gaps = rng.exponential(1.0, n_requests)
+    arrivals = np.cumsum(gaps) / rate
+    return [(float(a), int(rng.choice(SERVE_SIZES)), float(rng.uniform(0.1, 0.6))) for a in arrivals]
+
+
+def serving_physics(ma):
+    return ma.Options(problem_type=1, second_order_space=1, viscous=1, limiter=ma.MA_LIMITER_VANALBADA,
                       viscosity_model=ma.MA_VISC_CONSTANT, mu=1.8e-5, prandtl=0.72, precision=ma.MA_PREC_MIXED,
                       cfl=0.5)
-    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_requests))
-    reqs = [(float(a), int(rng.choice(sizes)), float(rng.uniform(0.1, 0.6))) for a in arrivals]
-    static = run_static_batch(ma, phys, reqs, budget)
+
+
+def run_serving(ma, reqs, static, budget=150 << 30, tick=25, max_running_cells=8_000_000, nsteps=SERVE_STEPS):
+    """Serves the requests (arrival offset s, n, Mach) through ma.Server:
+    admitted under the HBM budget with at most max_running_cells cells
+    running at once (the latency control: it bounds how many requests share
+    a tick), run with the launch shapes the autotuner picked for the same
+    requests as one static batch (tuned once for the workload, before the
+    stream starts). Latency = finish - submit per request."""
+    phys = serving_physics(ma)
     srv = ma.Server(phys, budget_bytes=budget, tick_steps=tick, capacity=512, thread=True)
     srv.set_max_running_cells(max_running_cells)
     srv.set_launch(*static["launch"])
     t0 = time.perf_counter()
-    for n in sizes:  # mesh cache warm-up: one device mesh per size
+    for n in sorted({n for _, n, _ in reqs}):  # mesh cache warm-up: one device mesh per size
         srv.preload(ma.Server.request(n, n, n, 2.0, 0.5, 0.5, flat_plate_inflow(0.3), nsteps))
     setup_s = time.perf_counter() - t0
     ids = []
@@ -664,13 +789,11 @@ def run_serving(ma, n_requests=32, rate=200.0, nsteps=500, seed=1, budget=150 <<
     queue = np.array([(i.t_admit_ns - i.t_submit_ns) / 1e9 for i in infos])
     done = sum(1 for i in infos if i.state == 2)
     cell_stages = sum(i.cells * 4 * nsteps for i in infos if i.state == 2)
-    offered = sum(n ** 3 * 4 * nsteps for _, n, _ in reqs) / (reqs[-1][0] if reqs[-1][0] > 0 else 1.0)
-    return {"workload": "Poisson %.0f/s flat-plate requests, Mach U[0.1,0.6], sizes {32..128}^3, %d steps, mixed"
-                        % (rate, nsteps),
-            "requests": n_requests, "completed": done, "tick_steps": tick, "budget_bytes": budget,
-            "launch": {"block": static["launch"][0], "grid": static["launch"][1]},
-            "max_running_cells": max_running_cells,
-            "mesh_cache_setup_s": setup_s,
+    span = reqs[-1][0] if reqs[-1][0] > 0 else 1.0
+    offered = sum(n ** 3 * 4 * nsteps for _, n, _ in reqs) / span
+    return {"requests": len(reqs), "completed": done, "tick_steps": tick, "budget_bytes": budget,
+            "max_running_cells": max_running_cells, "mesh_cache_setup_s": setup_s,
+            "offered_load_mcell_stage_s": offered / 1e6,
             "throughput": {"value": cell_stages / wall / 1e6, "unit": "Mcell-stage/s (wall, first arrival to last)"},
             "throughput_busy": {"value": st["cell_stages"] / max(st["busy_seconds"], 1e-9) / 1e6,
                                 "unit": "Mcell-stage/s (while requests run)"},
@@ -678,10 +801,40 @@ def run_serving(ma, n_requests=32, rate=200.0, nsteps=500, seed=1, budget=150 <<
                           "max": float(lat.max())},
             "queue_wait_s": {"p50": float(np.percentile(queue, 50)), "p99": float(np.percentile(queue, 99))},
             "peak_running": st["peak_running"], "peak_bytes": st["peak_bytes"],
-            "offered_load_mcell_stage_s": offered / 1e6,
             "saturated": bool(offered / 1e6 > cell_stages / wall / 1e6),
-            "batched_same_requests": static,
             "serving_vs_batched": (cell_stages / wall / 1e6) / static["value"]}
+
+
+def run_serving_suite(ma, n_requests=32, rate=200.0, loads=(0.25, 0.5, 0.9), n_load_requests=16,
+                      budget=150 << 30):
+    """Serving at the configured saturating stream (Poisson 200/s, more work
+    offered than one GPU carries: throughput against the static batch) and at
+    offered loads of 25, 50 and 90 % of the static batch's throughput (same
+    request mix, seeded; latency below saturation)."""
+    phys = serving_physics(ma)
+    sat_reqs = serving_requests(ma, n_requests, rate)
+    static = run_static_batch(ma, phys, sat_reqs, budget)
+    mean_work = float(np.mean([n ** 3 for n in SERVE_SIZES])) * 4 * SERVE_STEPS  # cell-stages per request
+    out = {"workload": "Poisson arrivals of flat-plate requests, Mach U[0.1,0.6], sizes {32,48,64,96,128}^3, "
+                       "%d steps, mixed precision, 150 GiB budget" % SERVE_STEPS,
+           "launch": {"block": static["launch"][0], "grid": static["launch"][1]},
+           "batched_same_requests": static,
+           "latency_control": "max_running_cells caps the cells running at once; the HBM budget "
+                              "(150 GiB) never binds for these request sizes"}
+    out["saturating_200_per_s"] = run_serving(ma, sat_reqs, static, budget=budget)
+    for load in loads:
+        r = load * static["value"] * 1e6 / mean_work
+        out["load_%d_pct" % round(load * 100)] = dict(
+            run_serving(ma, serving_requests(ma, n_load_requests, r), static, budget=budget),
+            arrival_rate_per_s=r, target_load_of_static_batch=load)
+    summ = {}
+    for key in ["saturating_200_per_s"] + ["load_%d_pct" % round(x * 100) for x in loads]:
+        v = out[key]
+        summ[key] = {"thru": _r(v["throughput"]["value"]), "p50_s": _r(v["latency_s"]["p50"], 3),
+                     "p99_s": _r(v["latency_s"]["p99"], 3), "vs_batched": _r(v["serving_vs_batched"], 3)}
+    summ["static_batch"] = _r(static["value"])
+    out["summary"] = summ
+    return out
 
 
 def run_static_batch(ma, phys, reqs, budget, steps=40, warmup=3, tune_after=25):
@@ -732,7 +885,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="all", choices=["all"] + sorted(WORKLOADS),
+                    help="all: the configuration suite (small Sod, Sod 256x128x128 as the headline, flat plate); "
+                         "the reference arm times the headline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the batched and serving sections")
     ap.add_argument("--serve-requests", type=int, default=32)
@@ -741,6 +896,8 @@ def main():
         args.warmup = 3
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
+        if args.workload == "all":
+            args.workload = DEFAULT_WORKLOAD
         run_reference(args, world, rank)
     else:
         run_ours(args, world, rank, local)

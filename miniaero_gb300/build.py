@@ -22,6 +22,11 @@ ORACLE_BUILD = os.path.join(ORACLE, "_build")
 LIB = os.path.join(BUILD, "libminiaero_gpu.so")
 CLI = os.path.join(BUILD, "miniaero")
 ORACLE_LIB = os.path.join(ORACLE_BUILD, "libminiaero_oracle.so")
+# The same oracle source built the way the reference's Makefile builds its
+# code (-O3 -g, the compiler's default contraction of a*b+c, which aarch64 g++
+# turns into fused multiply-adds): the CPU timing baseline only. Its sums are
+# not the reference's serial bits, so parity checks use ORACLE_LIB.
+ORACLE_TIMING_LIB = os.path.join(ORACLE_BUILD, "libminiaero_oracle_timing.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off"] + ARCH
@@ -78,6 +83,8 @@ def build(verbose=False, ptxas_info=False):
         jobs.append(HOST_CXX + ["-I" + cuda_include, "-c", os.path.join(CSRC, src), "-o", _obj(src)])
     jobs.append(["gcc", "-O2", "-std=c11", "-fPIC", "-ffp-contract=off", "-fopenmp", "-shared",
                  os.path.join(ORACLE, "miniaero_oracle.c"), "-o", ORACLE_LIB, "-lm"])
+    jobs.append(["gcc", "-O3", "-g", "-std=c11", "-fPIC", "-fopenmp", "-shared",
+                 os.path.join(ORACLE, "miniaero_oracle.c"), "-o", ORACLE_TIMING_LIB, "-lm"])
     outputs = []
     with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
         for out in ex.map(lambda c: _run(c, verbose), jobs):

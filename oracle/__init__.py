@@ -12,6 +12,9 @@ import numpy as np
 
 _DIR = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_DIR, "_build", "libminiaero_oracle.so")
+# The same source at -O3 with the compiler's default multiply-add contraction
+# (the reference Makefile's flags): CPU timing only, never a parity check.
+TIMING_LIB_PATH = os.path.join(_DIR, "_build", "libminiaero_oracle_timing.so")
 
 P_i32 = ctypes.POINTER(ctypes.c_int)
 P_f64 = ctypes.POINTER(ctypes.c_double)
@@ -35,15 +38,16 @@ class oracle_options(ctypes.Structure):
                 ("cell_flux", ctypes.c_int)]
 
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        if not os.path.exists(LIB_PATH):
-            raise ImportError("oracle library not built: %s" % LIB_PATH)
-        L = ctypes.CDLL(LIB_PATH)
+def lib(timing=False):
+    """The parity build (default) or, with timing=True, the -O3 timing build."""
+    path = TIMING_LIB_PATH if timing else LIB_PATH
+    if path not in _libs:
+        if not os.path.exists(path):
+            raise ImportError("oracle library not built: %s" % path)
+        L = ctypes.CDLL(path)
         L.oracle_solve.restype = ctypes.c_int
         L.oracle_solve.argtypes = [ctypes.POINTER(oracle_mesh), ctypes.POINTER(oracle_options), P_f64, P_f64,
                                    ctypes.c_int]
@@ -62,8 +66,8 @@ def lib():
         for name in ("oracle_field_gradients", "oracle_field_limiter", "oracle_field_bc_flux"):
             getattr(L, name).argtypes = [ctypes.POINTER(oracle_mesh), ctypes.POINTER(oracle_options), P_f64, P_f64]
             getattr(L, name).restype = ctypes.c_int
-        _lib = L
-    return _lib
+        _libs[path] = L
+    return _libs[path]
 
 
 def _p(a, t):
@@ -122,26 +126,28 @@ def _c_options(options, nsteps=None, dt=None):
 class Stepper:
     """Persistent oracle state advanced step by step (CPU baseline timing)."""
 
-    def __init__(self, md, options, U0, dt=None, nthreads=1):
+    def __init__(self, md, options, U0, dt=None, nthreads=1, timing=False):
         self.mesh = OracleMesh(md)
         self.opts = _c_options(options, 0, dt)
         self.ncells = md.ncells
+        self.L = lib(timing)
         U0 = np.ascontiguousarray(U0, dtype=np.float64)
-        self.h = lib().oracle_create(ctypes.byref(self.mesh.c), ctypes.byref(self.opts), _p(U0, P_f64), int(nthreads))
+        self.h = self.L.oracle_create(ctypes.byref(self.mesh.c), ctypes.byref(self.opts), _p(U0, P_f64),
+                                      int(nthreads))
         if not self.h:
             raise RuntimeError("oracle_create failed")
 
     def step(self, n=1):
-        lib().oracle_step(self.h, int(n))
+        self.L.oracle_step(self.h, int(n))
 
     def state(self):
         U = np.empty((self.ncells, 5))
-        lib().oracle_get_state(self.h, _p(U, P_f64), ctypes.cast(None, P_f64))
+        self.L.oracle_get_state(self.h, _p(U, P_f64), ctypes.cast(None, P_f64))
         return U
 
     def close(self):
         if self.h:
-            lib().oracle_free(self.h)
+            self.L.oracle_free(self.h)
             self.h = None
 
     def __del__(self):

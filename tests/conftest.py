@@ -31,7 +31,7 @@ def _sources_newer_than(target):
 def built():
     """Builds the library and the oracle once if they are missing or stale."""
     from miniaero_gb300 import build as b
-    if _sources_newer_than(b.LIB) or _sources_newer_than(b.ORACLE_LIB):
+    if any(_sources_newer_than(t) for t in (b.LIB, b.ORACLE_LIB, b.ORACLE_TIMING_LIB)):
         b.build()
     return True
 

@@ -130,3 +130,31 @@ def test_uniform_flow_is_preserved_at_eight_million_cells(has_gpu):
     scale = np.abs(U0).max(axis=0)
     scale[1:4] = scale[1:4].max()
     assert np.max(np.abs(U - U0) / scale) <= 1e-12
+
+
+@pytest.mark.parametrize("name,steps", [("sod_2nd_viscous_256x128x128", 100),
+                                        ("flat_plate_vanalbada_512x128x128", 50)])
+def test_mixed_form_error_at_the_configured_step_count(has_gpu, name, steps):
+    """The benchmark configurations at their own step counts (100 RK4 steps
+    for the Sod mesh, 50 for the flat plate) and CFL 0.5 dt: the mixed form's
+    relative L2 density error against the GPU's FP64 result (which equals the
+    reference's bits) stays within 1e-5. All five variables are reported;
+    momentum components relative to the momentum norm."""
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "full_size.json")) as f:
+        case = json.load(f)["cases"][name]
+    o = ma.Options(**case["options"])
+    md = ma.Parallel3DMesh.from_options(o).fill_mesh_data()
+    dm = ma.DeviceMesh(md)
+    a = run(md, o, steps=steps, device_mesh=dm)
+    om = o.copy()
+    om.precision = ma.MA_PREC_MIXED
+    b = run(md, om, steps=steps, device_mesh=dm)
+    dm.close()
+    mom = np.linalg.norm(a[:, 1:4])
+    err = [float(np.linalg.norm(b[:, k] - a[:, k]) / (mom if k in (1, 2, 3) else np.linalg.norm(a[:, k])))
+           for k in range(5)]
+    print("%s after %d steps: rel L2 error rho %.3e, rho u/v/w %.3e %.3e %.3e (of |rho u|), rho E %.3e"
+          % (name, steps, *err))
+    assert err[0] <= 1e-5, err

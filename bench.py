@@ -200,7 +200,7 @@ def make_options(ma, name, precision="fp64"):
     if name.startswith("flat_plate"):
         o.inflow_state = flat_plate_inflow()
         o.inflow_given = 1
-    o.precision = ma.MA_PREC_MIXED if precision == "mixed" else ma.MA_PREC_FP64
+    o.precision = {"mixed": ma.MA_PREC_MIXED, "fp64_fma": ma.MA_PREC_FP64_FMA}.get(precision, ma.MA_PREC_FP64)
     return o
 
 
@@ -382,10 +382,28 @@ def measure_config(ma, args, world, rank, local, name, err_steps, timed_steps, c
     mms = allreduce_max(world, time_steps(ma, msolver, timed_steps))
     mvalue = world * C * 4 * timed_steps / (mms / 1e3) / 1e6
     mprof = msolver.profile_steps(2)
+    msolver.close()
+    # ---- the opt-in contracted FP64 form: throughput and deviation from the bits ----
+    fo = make_options(ma, name, "fp64_fma")
+    fsolver = ma.TimeSolverExplicitRK4(md, fo, device_mesh=dmesh)
+    fsolver.set_state(U0)
+    fsolver.dt = dt
+    fsolver.step(err_steps)
+    fsolver.synchronize()
+    U_fma = fsolver.get_state()
+    scale = np.abs(U_fp64).max(axis=0)
+    scale[1:4] = scale[1:4].max()
+    fma_err = (np.abs(U_fma - U_fp64).max(axis=0) / scale).tolist()
+    fsolver.set_state(U_start)
+    fsolver.dt = dt
+    fsolver.step(args.warmup)
+    fsolver.synchronize()
+    fms = allreduce_max(world, time_steps(ma, fsolver, timed_steps))
+    fvalue = world * C * 4 * timed_steps / (fms / 1e3) / 1e6
+    fsolver.close()
     mroofline, mkernels = kernel_rooflines(md, mprof, 4, clocks.get("sm_mhz"), None, counted, second_viscous,
                                            "traffic_bytes_per_launch_mixed" if scaled else None)
     mroofline["stage"] = stage_roofline(C, mprof, 4) if second_viscous else None
-    msolver.close()
 
     # ---- end to end through the C ABI with pinned host buffers ----
     eo = make_options(ma, name, "fp64")
@@ -444,11 +462,45 @@ def measure_config(ma, args, world, rank, local, name, err_steps, timed_steps, c
                   "speedup_vs_fp64": mvalue / value, "rel_l2_error_vs_fp64": errs,
                   "error_note": "momentum components relative to the momentum norm",
                   "error_after_steps": err_steps, "roofline": mroofline, "kernels": mkernels},
+        "fp64_fma": {"value": fvalue, "unit": "Mcell-stage/s", "ms_per_step": fms / timed_steps,
+                     "speedup_vs_fp64": fvalue / value, "max_rel_error_vs_fp64": fma_err,
+                     "error_note": "max over cells of |U_fma - U_fp64| over each variable's largest magnitude "
+                                   "(momentum components share one scale)",
+                     "error_after_steps": err_steps},
         "cpu_baseline": cpu_results.get("timing"),
     }
     if "parity" in cpu_results:
         res["cpu_baseline_parity_build"] = cpu_results["parity"]
     return res
+
+
+def one_launch_value(ma, name, steps, warmup):
+    """The configuration as a one-member batch in single-launch mode: all
+    `steps` RK4 steps in one cooperative launch (no per-kernel launches)."""
+    import torch
+    out = {}
+    for prec_name in ("fp64", "mixed"):
+        o = make_options(ma, name, prec_name)
+        md = ma.Parallel3DMesh.from_options(o).fill_mesh_data()
+        U0 = ma.initial_state(md, o)
+        dm = ma.DeviceMesh(md)
+        b = ma.Batch(o, capacity=1, budget_bytes=64 << 30)
+        grid = b.set_single_launch(256)
+        b.add(dm, U0)
+        b.step(warmup)
+        b.synchronize()
+        stream = torch.cuda.ExternalStream(b.stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.step(steps)
+        e1.record(stream)
+        b.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[prec_name] = {"value": md.ncells * 4 * steps / (ms / 1e3) / 1e6, "unit": "Mcell-stage/s",
+                          "steps": steps, "launches": 1, "block": 256, "grid": grid}
+        b.close()
+        dm.close()
+    return out
 
 
 def _r(x, n=4):
@@ -466,9 +518,13 @@ def compact(name, r):
     out = {"cells": r["config"]["cells"], "timed_steps": r["timed_steps"], "fp64": _r(r["value"]),
            "e2e": _r(r["e2e"]["value"]), "cpu": _r(cpu.get("value")),
            "e2e_vs_cpu": _r(r["e2e"]["value"] / cpu["value"]) if cpu.get("value") else None,
+           "fp64_fma": _r(r["fp64_fma"]["value"]), "fma_err": _r(max(r["fp64_fma"]["max_rel_error_vs_fp64"]), 2),
            "mixed": _r(r["mixed"]["value"]), "mixed_speedup": _r(r["mixed"]["speedup_vs_fp64"]),
            "mixed_err": [_r(e, 2) for e in r["mixed"]["rel_l2_error_vs_fp64"]],
            "err_steps": r["mixed"]["error_after_steps"]}
+    if r.get("one_launch"):
+        out["fp64_one_launch"] = _r(r["one_launch"]["fp64"]["value"])
+        out["mixed_one_launch"] = _r(r["one_launch"]["mixed"]["value"])
     if st:
         out["stage_hbm_frac"] = _r(st["frac"], 3)
     if mst:
@@ -494,6 +550,10 @@ def run_ours(args, world, rank, local):
             timed, cpu = max(args.steps, err_steps), ("timing",)
         results[name] = measure_config(ma, args, world, rank, local, name, err_steps, timed, cpu,
                                        cpu_seconds=(12.0 if name == headline else 8.0))
+        if results[name]["config"]["cells"] < 1_000_000:
+            # A small mesh is launch- and latency-sensitive: also time it as
+            # one cooperative launch for all its steps.
+            results[name]["one_launch"] = one_launch_value(ma, name, timed, args.warmup)
 
     batched = serving = None
     if not args.no_extras:
@@ -519,8 +579,10 @@ def run_ours(args, world, rank, local):
         # key numbers of every configuration, the batch and the serving loads.
         summary = {n: compact(n, r) for n, r in results.items()}
         if batched:
-            summary["batched_64_sod_boxes"] = {"fp64": _r(batched["fp64"]["value"]),
-                                               "mixed": _r(batched["mixed"]["value"])}
+            summary["batched_64_sod_boxes"] = {
+                "fp64": _r(batched["fp64"]["value"]), "mixed": _r(batched["mixed"]["value"]),
+                "fp64_one_launch": _r(batched["fp64"]["single_launch"]["value"]),
+                "mixed_one_launch": _r(batched["mixed"]["single_launch"]["value"])}
         if serving:
             summary["serving"] = serving["summary"]
         line["summary"] = summary
@@ -724,7 +786,22 @@ def run_batched(ma, steps, warmup, n_members=64):
             seq_ms += a0.elapsed_time(a1)
             s.close()
         block, grid = b.launch
+        # The same steps as one cooperative launch (all steps, all members).
+        sgrid = b.set_single_launch(256)
+        b.step(1)
+        b.synchronize()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        b.step(steps)
+        s1.record(stream)
+        b.synchronize()
+        sms = s0.elapsed_time(s1)
+        b.set_single_launch(0)
+        b.set_launch(block, grid)
         res[prec_name] = {"value": cells * 4 * steps / (ms / 1e3) / 1e6, "unit": "Mcell-stage/s",
+                          "single_launch": {"value": cells * 4 * steps / (sms / 1e3) / 1e6,
+                                            "unit": "Mcell-stage/s", "launches": 1, "steps_per_launch": steps,
+                                            "block": 256, "grid": sgrid},
                           "ms_per_step": ms / steps,
                           "sequential_single_mesh_value": cells * 4 * steps / (seq_ms / 1e3) / 1e6,
                           "autotuned": {"block": block, "grid": grid, "ms_per_launch": tuned.tolist()},

@@ -39,7 +39,17 @@ typedef enum {
 enum { MA_BC_EXTRAPOLATE = 0, MA_BC_TANGENT = 1, MA_BC_INFLOW = 2, MA_BC_NOSLIP = 3 };
 enum { MA_LIMITER_VENKAT = 0, MA_LIMITER_VANALBADA = 1 };
 enum { MA_VISC_SUTHERLAND = 0, MA_VISC_CONSTANT = 1 };
-enum { MA_PREC_FP64 = 0, MA_PREC_MIXED = 1 };
+/* MA_PREC_FP64: the reference's serial arithmetic, bit for bit.
+ * MA_PREC_MIXED: FP32 flux, gradient and limiter; FP64 residual sum and RK4
+ * update (relative L2 density error <= 1e-5 against FP64).
+ * MA_PREC_FP64_FMA: the FP64 kernels with a*b+c fused where the compiler
+ * contracts it (as an aarch64 build of the reference with default flags
+ * does); same summation orders, round-off-level differences from the
+ * reference's bits that grow with the flow (opt-in; within 1e-12 on the
+ * benchmark meshes after their configured steps, 7e-9 after the reference's
+ * 400-step flat plate, where its own serial and threaded builds differ as
+ * much). */
+enum { MA_PREC_FP64 = 0, MA_PREC_MIXED = 1, MA_PREC_FP64_FMA = 2 };
 enum { MA_GATHER_ATOMICS = 0, MA_GATHER_CELL_FLUX = 1 };
 /* State layouts: AOS is View<double*[5]> LayoutRight (U[c*5+k], the
  * reference's host layout); SOA is U[k*ncells+c]. */
@@ -270,6 +280,15 @@ ma_status ma_batch_remove(ma_batch* b, int32_t member_id);
 ma_status ma_batch_get_state(ma_batch* b, int32_t member_id, double* U, int32_t layout);
 /* Advances every member nsteps RK4 steps (asynchronous). */
 ma_status ma_batch_step(ma_batch* b, int32_t nsteps);
+/* Single-launch mode: with block > 0 (64..256, a multiple of 32), every
+ * ma_batch_step(b, n) runs all n RK4 steps of every member as ONE
+ * cooperative kernel launch of `block` threads x as many blocks as fit on the
+ * device at once (written to *grid_out when not NULL): the stage kernels
+ * become phases of one persistent kernel, separated by a grid barrier whose
+ * waits are bounded (ma_batch_synchronize then returns MA_ETIMEDOUT). Every
+ * kind's chunks take `block` items. Same bits as the per-kind launches;
+ * block = 0 returns to those (captured in a CUDA graph per step). */
+ma_status ma_batch_set_single_launch(ma_batch* b, int32_t block, int32_t* grid_out);
 ma_status ma_batch_synchronize(ma_batch* b);
 void* ma_batch_stream(ma_batch* b);
 int64_t ma_batch_cells(ma_batch* b);

@@ -23,7 +23,7 @@ import numpy as np
 from . import _lib
 from ._lib import (MA_BC_EXTRAPOLATE, MA_BC_INFLOW, MA_BC_NOSLIP, MA_BC_TANGENT, MA_IC_CONSTANT,
                    MA_IC_REFERENCE, MA_IC_SOD, MA_LAYOUT_AOS, MA_LAYOUT_SOA, MA_LIMITER_VANALBADA,
-                   MA_LIMITER_VENKAT, MA_PREC_FP64, MA_PREC_MIXED, MA_VISC_CONSTANT, MA_VISC_SUTHERLAND,
+                   MA_LIMITER_VENKAT, MA_PREC_FP64, MA_PREC_FP64_FMA, MA_PREC_MIXED, MA_VISC_CONSTANT, MA_VISC_SUTHERLAND,
                    MiniaeroError, check, f64p, i32p, lib)
 
 __all__ = [
@@ -33,7 +33,7 @@ __all__ = [
     "device_count", "MiniaeroError", "BC_NAMES",
     "MA_BC_EXTRAPOLATE", "MA_BC_TANGENT", "MA_BC_INFLOW", "MA_BC_NOSLIP",
     "MA_LIMITER_VENKAT", "MA_LIMITER_VANALBADA", "MA_VISC_SUTHERLAND", "MA_VISC_CONSTANT",
-    "MA_PREC_FP64", "MA_PREC_MIXED", "MA_IC_REFERENCE", "MA_IC_SOD", "MA_IC_CONSTANT",
+    "MA_PREC_FP64", "MA_PREC_MIXED", "MA_PREC_FP64_FMA", "MA_IC_REFERENCE", "MA_IC_SOD", "MA_IC_CONSTANT",
     "MA_LAYOUT_AOS", "MA_LAYOUT_SOA",
 ]
 
@@ -412,6 +412,14 @@ class Batch:
 
     def step(self, nsteps=1):
         check(lib().ma_batch_step(self._h, int(nsteps)))
+
+    def set_single_launch(self, block=256):
+        """block > 0: each step() call runs as one cooperative launch (all
+        steps, all members); 0: per-kind launches in a CUDA graph. Returns
+        the launch's grid (0 when off)."""
+        grid = ctypes.c_int32(0)
+        check(lib().ma_batch_set_single_launch(self._h, int(block), ctypes.byref(grid)))
+        return grid.value
 
     def synchronize(self):
         check(lib().ma_batch_synchronize(self._h))

@@ -13,7 +13,7 @@ MA_OK, MA_EINVAL, MA_ENOMEM, MA_ECUDA, MA_EBUDGET, MA_ETIMEDOUT, MA_ENUMERIC, MA
 MA_BC_EXTRAPOLATE, MA_BC_TANGENT, MA_BC_INFLOW, MA_BC_NOSLIP = range(4)
 MA_LIMITER_VENKAT, MA_LIMITER_VANALBADA = 0, 1
 MA_VISC_SUTHERLAND, MA_VISC_CONSTANT = 0, 1
-MA_PREC_FP64, MA_PREC_MIXED = 0, 1
+MA_PREC_FP64, MA_PREC_MIXED, MA_PREC_FP64_FMA = 0, 1, 2
 MA_GATHER_ATOMICS, MA_GATHER_CELL_FLUX = 0, 1
 MA_MESH_CELL_FLUX = 1
 MA_LAYOUT_AOS, MA_LAYOUT_SOA = 0, 1
@@ -202,6 +202,7 @@ _SIGNATURES = {
     "ma_batch_member_dt": (c_double, [c_void_p, c_int32]),
     "ma_batch_get_launch": (c_int32, [c_void_p, P_i32, P_i32]),
     "ma_batch_set_launch": (c_int32, [c_void_p, P_i32, P_i32]),
+    "ma_batch_set_single_launch": (c_int32, [c_void_p, c_int32, P_i32]),
     "ma_batch_autotune": (c_int32, [c_void_p, c_int32, P_f64]),
     "ma_batch_profile_steps": (c_int32, [c_void_p, c_int32, P_f64, P_i32]),
     "ma_server_create": (c_int32, [ctypes.POINTER(ma_options), ctypes.c_size_t, c_int32, c_int32, c_int32,

@@ -35,6 +35,8 @@ HOST_CXX = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall"]
 # (source, extra flags)
 DEVICE_SOURCES = [
     ("device/kernels_fp64.cu", ["--fmad=false"]),
+    # The opt-in contracted FP64 form (MA_PREC_FP64_FMA).
+    ("device/kernels_fp64_fma.cu", ["--fmad=true"]),
     # FP32 division and square root as the full-range approximations (within
     # 2 ulp): the IEEE forms' slow-path branches cost the mixed sweep 16 % and
     # the mixed flux 6 %, and the mixed form keeps no reference bits.

@@ -64,6 +64,7 @@ struct ma_batch {
   ma_options opts;
   dev::PathConfig cfg;
   bool mixed = false;
+  bool fma = false;  // MA_PREC_FP64_FMA
   int32_t capacity = 0;
   size_t budget = 0;
   size_t used = 0;
@@ -84,6 +85,12 @@ struct ma_batch {
   int64_t cells = 0;
   unsigned long long* d_scratch = nullptr;
   int sm_count = 0;
+  // Single-launch mode (ma_batch_set_single_launch): a whole ma_batch_step is
+  // one cooperative launch of `single_block` x `single_grid`.
+  int single_block = 0;  // 0: per-kind launches captured in a graph
+  int single_grid = 0;
+  unsigned* d_barrier = nullptr;  // two words: arrival count, generation
+  int* d_err = nullptr;           // set by a grid barrier that gave up
 };
 
 namespace {
@@ -165,13 +172,46 @@ ma_status launch_stage_on(ma_batch* b, int stage, unsigned kernels, cudaStream_t
   cudaError_t e = b->mixed
       ? dev::launch_batch_stage<float>(b->cfg, static_cast<const dev::Segment<float>*>(b->d_segs), b->launch, stage,
                                        stream, kernels)
-      : dev::launch_batch_stage<double>(b->cfg, static_cast<const dev::Segment<double>*>(b->d_segs), b->launch, stage,
-                                        stream, kernels);
+      : b->fma ? dev::launch_batch_stage_fma(b->cfg, static_cast<const dev::Segment<double>*>(b->d_segs), b->launch,
+                                             stage, stream, kernels)
+               : dev::launch_batch_stage<double>(b->cfg, static_cast<const dev::Segment<double>*>(b->d_segs),
+                                                 b->launch, stage, stream, kernels);
   if (e != cudaSuccess) return set_error(MA_ECUDA, std::string("batch stage launch: ") + cudaGetErrorString(e));
   return MA_OK;
 }
 
 ma_status launch_stage(ma_batch* b, int stage, unsigned kernels) { return launch_stage_on(b, stage, kernels, b->stream); }
+
+// nsteps whole steps as one cooperative launch (single-launch mode).
+ma_status launch_steps_single(ma_batch* b, int32_t nsteps) {
+  for (int k = 0; k < 4; ++k)
+    if (b->launch.block[k] != b->single_block)
+      return set_error(MA_ESTATE, "ma_batch_step: launch shapes changed after ma_batch_set_single_launch; set it again");
+  cudaError_t e;
+  if (b->mixed)
+    e = dev::launch_batch_steps_mixed(b->cfg, b->d_segs, b->launch, nsteps, b->d_barrier, b->d_err, b->single_block,
+                                      b->single_grid, b->stream);
+  else if (b->fma)
+    e = dev::launch_batch_steps_fp64_fma(b->cfg, b->d_segs, b->launch, nsteps, b->d_barrier, b->d_err,
+                                         b->single_block, b->single_grid, b->stream);
+  else
+    e = dev::launch_batch_steps_fp64(b->cfg, b->d_segs, b->launch, nsteps, b->d_barrier, b->d_err, b->single_block,
+                                     b->single_grid, b->stream);
+  if (e != cudaSuccess) return set_error(MA_ECUDA, std::string("batch single launch: ") + cudaGetErrorString(e));
+  return MA_OK;
+}
+
+// After the stream has drained: MA_ETIMEDOUT if a grid barrier of the
+// single-launch kernel gave up (the flag is cleared).
+ma_status check_barrier_error(ma_batch* b) {
+  if (!b->single_block) return MA_OK;
+  int err = 0;
+  MB_CUDA_TRY(cudaMemcpy(&err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err == 0) return MA_OK;
+  MB_CUDA_TRY(cudaMemset(b->d_barrier, 0, 2 * sizeof(unsigned) + sizeof(int)));
+  return set_error(MA_ETIMEDOUT, "ma_batch_step: a grid barrier of the single-launch step timed out; member states "
+                                 "are incomplete");
+}
 
 ma_status capture_graph(ma_batch* b) {
   drop_graph(b);
@@ -217,13 +257,15 @@ void default_grid(ma_batch* b) {
 extern "C" ma_status ma_batch_create(const ma_options* o, int32_t capacity, size_t budget_bytes, ma_batch** out) {
   if (!o || !out || capacity <= 0) return set_error(MA_EINVAL, "ma_batch_create: bad arguments");
   *out = nullptr;
-  if (o->precision != MA_PREC_FP64 && o->precision != MA_PREC_MIXED) return set_error(MA_EINVAL, "bad precision");
+  if (o->precision != MA_PREC_FP64 && o->precision != MA_PREC_MIXED && o->precision != MA_PREC_FP64_FMA)
+    return set_error(MA_EINVAL, "bad precision");
   if (o->gather != MA_GATHER_ATOMICS && o->gather != MA_GATHER_CELL_FLUX) return set_error(MA_EINVAL, "bad gather");
   // A failure part way releases what was created (ma_batch_free skips null handles).
   std::unique_ptr<ma_batch, void (*)(ma_batch*)> b(new (std::nothrow) ma_batch, ma_batch_free);
   if (!b) return set_error(MA_ENOMEM, "ma_batch_create: out of host memory");
   b->opts = *o;
   b->mixed = o->precision == MA_PREC_MIXED;
+  b->fma = o->precision == MA_PREC_FP64_FMA;
   b->cfg.second_order = o->second_order_space != 0;
   b->cfg.viscous = o->viscous != 0;
   b->cfg.limiter = o->limiter;
@@ -235,9 +277,12 @@ extern "C" ma_status ma_batch_create(const ma_options* o, int32_t capacity, size
   MB_CUDA_TRY(cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, b->device));
   const size_t seg_size = b->mixed ? sizeof(dev::Segment<float>) : sizeof(dev::Segment<double>);
   MB_CUDA_TRY(cudaMalloc(&b->d_segs, seg_size * capacity));
-  MB_CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&b->d_nchunks), 4 * sizeof(int) + 8));
-  MB_CUDA_TRY(cudaMemset(b->d_nchunks, 0, 4 * sizeof(int) + 8));
+  // [0, 16) chunk counts, [16, 24) CFL scratch, [24, 32) grid barrier, [32, 36) barrier error.
+  MB_CUDA_TRY(cudaMalloc(reinterpret_cast<void**>(&b->d_nchunks), 64));
+  MB_CUDA_TRY(cudaMemset(b->d_nchunks, 0, 64));
   b->d_scratch = reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(b->d_nchunks) + 16);
+  b->d_barrier = reinterpret_cast<unsigned*>(reinterpret_cast<char*>(b->d_nchunks) + 24);
+  b->d_err = reinterpret_cast<int*>(reinterpret_cast<char*>(b->d_nchunks) + 32);
   MB_CUDA_TRY(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
   MB_CUDA_TRY(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
   MB_CUDA_TRY(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
@@ -335,6 +380,7 @@ extern "C" ma_status ma_batch_add(ma_batch* b, ma_mesh* mesh, const double* U0, 
     m.dt = b->opts.cfl * r;
   }
   e = b->mixed ? dev::launch_init_primitives<float>(t, m.st, m.b32, b->stream)
+      : b->fma ? dev::launch_init_primitives_fma(t, m.st, m.b64, b->stream)
                : dev::launch_init_primitives<double>(t, m.st, m.b64, b->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
   if (e != cudaSuccess) return fail(set_error(MA_ECUDA, std::string("ma_batch_add: ") + cudaGetErrorString(e)));
@@ -363,6 +409,9 @@ extern "C" ma_status ma_batch_get_state(ma_batch* b, int32_t id, double* U, int3
   auto it = b->members.find(id);
   if (it == b->members.end()) return set_error(MA_ENOTFOUND, "ma_batch_get_state: unknown member");
   const size_t C = miniaero::mesh_cells(it->second.mesh);
+  MB_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  ma_status bst = check_barrier_error(b);
+  if (bst != MA_OK) return bst;
   if (layout == MA_LAYOUT_SOA) {
     MB_CUDA_TRY(cudaMemcpyAsync(U, it->second.st.Un, 5 * C * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
     MB_CUDA_TRY(cudaStreamSynchronize(b->stream));
@@ -386,12 +435,47 @@ extern "C" ma_status ma_batch_step(ma_batch* b, int32_t nsteps) {
     ma_status st = upload_tables(b);
     if (st != MA_OK) return st;
   }
+  if (b->single_block) {
+    ma_status st = launch_steps_single(b, nsteps);
+    if (st != MA_OK) return st;
+    for (auto& kv : b->members) kv.second.steps += nsteps;
+    return MA_OK;
+  }
   if (!b->graph) {
     ma_status st = capture_graph(b);
     if (st != MA_OK) return st;
   }
   for (int32_t i = 0; i < nsteps; ++i) MB_CUDA_TRY(cudaGraphLaunch(b->graph, b->stream));
   for (auto& kv : b->members) kv.second.steps += nsteps;
+  return MA_OK;
+}
+
+extern "C" ma_status ma_batch_set_single_launch(ma_batch* b, int32_t block, int32_t* grid_out) {
+  if (!b) return set_error(MA_EINVAL, "ma_batch_set_single_launch: null batch");
+  if (block != 0 && (block < 64 || block > 256 || block % 32))
+    return set_error(MA_EINVAL, "ma_batch_set_single_launch: block must be 0 (off) or 64..256 in steps of 32");
+  MB_CUDA_TRY(cudaSetDevice(b->device));
+  MB_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  if (block == 0) {
+    b->single_block = 0;
+    b->single_grid = 0;
+    if (grid_out) *grid_out = 0;
+    return MA_OK;
+  }
+  int per_sm = 0;
+  cudaError_t e = b->mixed ? dev::batch_steps_occupancy_mixed(b->cfg, block, &per_sm)
+                  : b->fma ? dev::batch_steps_occupancy_fp64_fma(b->cfg, block, &per_sm)
+                           : dev::batch_steps_occupancy_fp64(b->cfg, block, &per_sm);
+  if (e != cudaSuccess) return set_error(MA_ECUDA, std::string("ma_batch_set_single_launch: ") + cudaGetErrorString(e));
+  if (per_sm < 1) return set_error(MA_EINVAL, "ma_batch_set_single_launch: the kernel does not fit on an SM at this block size");
+  // Every kind's chunks must match the one block size of the launch.
+  for (int k = 0; k < 4; ++k) b->launch.block[k] = block;
+  b->single_block = block;
+  b->single_grid = per_sm * b->sm_count;
+  b->tables_dirty = true;
+  drop_graph(b);
+  MB_CUDA_TRY(cudaMemset(b->d_barrier, 0, 2 * sizeof(unsigned) + sizeof(int)));
+  if (grid_out) *grid_out = b->single_grid;
   return MA_OK;
 }
 
@@ -453,7 +537,7 @@ extern "C" ma_status ma_batch_profile_steps(ma_batch* b, int32_t nsteps, double*
 extern "C" ma_status ma_batch_synchronize(ma_batch* b) {
   if (!b) return set_error(MA_EINVAL, "ma_batch_synchronize: null batch");
   MB_CUDA_TRY(cudaStreamSynchronize(b->stream));
-  return MA_OK;
+  return check_barrier_error(b);
 }
 
 extern "C" void* ma_batch_stream(ma_batch* b) { return b ? static_cast<void*>(b->stream) : nullptr; }

@@ -124,6 +124,16 @@ template <>
 cudaError_t launch_stage<float>(const TopoView&, const GeomView<float>&, const PathConfig&, const StateBuffers&,
                                 const StageBuffers<float>&, int, cudaStream_t, unsigned);
 
+// The FP64 form built with multiply-add contraction (kernels_fp64_fma.cu,
+// --fmad=true): the same kernels and summation orders as launch_stage<double>,
+// with a*b+c rounded once where the compiler fuses it. Not the reference's
+// bits; the opt-in MA_PREC_FP64_FMA precision.
+cudaError_t launch_init_primitives_fma(const TopoView& t, const StateBuffers& s, const StageBuffers<double>& b,
+                                       cudaStream_t stream);
+cudaError_t launch_stage_fma(const TopoView& t, const GeomView<double>& g, const PathConfig& cfg,
+                             const StateBuffers& s, const StageBuffers<double>& b, int stage, cudaStream_t stream,
+                             unsigned kernels = kAllKernels);
+
 // Batched stage over segments: chunks[k] lists (segment, first item) pairs of
 // kernel kind k (sweep, internal flux, boundary flux, residual), each chunk
 // covering block[k] items; nchunks is a device array of 4 counts.
@@ -143,6 +153,25 @@ cudaError_t launch_batch_stage<double>(const PathConfig&, const Segment<double>*
 template <>
 cudaError_t launch_batch_stage<float>(const PathConfig&, const Segment<float>*, const BatchLaunch&, int,
                                       cudaStream_t, unsigned);
+cudaError_t launch_batch_stage_fma(const PathConfig& cfg, const Segment<double>* segs, const BatchLaunch& bl,
+                                   int stage, cudaStream_t stream, unsigned kernels = kAllKernels);
+
+// Whole batch steps as one cooperative launch (kb_steps): nsteps RK4 steps of
+// every member, the phases of each stage separated by a bounded grid barrier.
+// The chunk tables must use one chunk size, `block` (the launch's block
+// size); grid must not exceed the resident blocks (batch_steps_occupancy
+// times the SM count). barrier_words: two zeroed device words; *err is set
+// when a barrier wait gave up. One function per precision (the translation
+// unit that builds it).
+cudaError_t launch_batch_steps_fp64(const PathConfig& cfg, const void* segs, const BatchLaunch& bl, int nsteps,
+                                    unsigned* barrier_words, int* err, int block, int grid, cudaStream_t stream);
+cudaError_t launch_batch_steps_mixed(const PathConfig& cfg, const void* segs, const BatchLaunch& bl, int nsteps,
+                                     unsigned* barrier_words, int* err, int block, int grid, cudaStream_t stream);
+cudaError_t launch_batch_steps_fp64_fma(const PathConfig& cfg, const void* segs, const BatchLaunch& bl, int nsteps,
+                                        unsigned* barrier_words, int* err, int block, int grid, cudaStream_t stream);
+cudaError_t batch_steps_occupancy_fp64(const PathConfig& cfg, int block, int* blocks_per_sm);
+cudaError_t batch_steps_occupancy_mixed(const PathConfig& cfg, int block, int* blocks_per_sm);
+cudaError_t batch_steps_occupancy_fp64_fma(const PathConfig& cfg, int block, int* blocks_per_sm);
 
 // dt bound of the CFL rule: writes min_c V_c / sum_f(|u.n| + c|n|) (as the
 // bits of a positive double) into *out via atomicMin; *out must start at ~0.

@@ -24,5 +24,15 @@ cudaError_t launch_batch_stage<double>(const PathConfig& cfg, const Segment<doub
   return launch_batch_stage_impl<double>(cfg, segs, bl, stage, stream, kernels);
 }
 
+cudaError_t launch_batch_steps_fp64(const PathConfig& cfg, const void* segs, const BatchLaunch& bl, int nsteps,
+                               unsigned* barrier_words, int* err, int block, int grid, cudaStream_t stream) {
+  return launch_batch_steps_impl<double>(cfg, static_cast<const Segment<double>*>(segs), bl, nsteps, barrier_words, err,
+                                     block, grid, stream);
+}
+
+cudaError_t batch_steps_occupancy_fp64(const PathConfig& cfg, int block, int* blocks_per_sm) {
+  return batch_steps_occupancy_impl<double>(cfg, block, blocks_per_sm);
+}
+
 }  // namespace dev
 }  // namespace miniaero

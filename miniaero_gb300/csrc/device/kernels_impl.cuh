@@ -39,6 +39,11 @@ constexpr int kSweepMinBlocks = std::is_same<R, float>::value ? 4 : 2;
 template <class R>
 constexpr int kFluxMinBlocks = std::is_same<R, float>::value ? 8 : 0;
 
+// Resident residual blocks per SM (0: no bound). The mixed residual holds a
+// cell's 30 face-flux words for its integer sums.
+template <class R>
+constexpr int kResidualMinBlocks = std::is_same<R, float>::value ? 0 : 0;
+
 // Primitives of an FP64 state written as R: FP64 arithmetic for the plain
 // form (bit-exact), FP32 for the mixed form (its flux work is FP32 anyway).
 template <class R>
@@ -711,8 +716,39 @@ __device__ __forceinline__ void residual_cell(const TopoView& t, const R* __rest
   // the mixed form multiplies by 1/V.
   const double dtv = std::is_same<R, double>::value ? div_by_recip(dt, t.vol[c], t.vinv[c]) : dt * t.vinv[c];
   double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  if constexpr (std::is_same<R, float>::value) {
+    if (!cell_flux) {
+      // Mixed form: each component's sum of the cell's FP32 face fluxes is
+      // the exact sum rounded once to FP64 (exact_sum_f32, integer pipe), not
+      // five FP64 additions; the FP64 pipe keeps the dt/V scaling and the
+      // RK4 update.
+      uint32_t bits[kMaxCellFaces][5];
+#pragma unroll
+      for (int s = 0; s < kMaxCellFaces; ++s) {
+        const int code = t.csr_flux[s * C + c];
+        const int f = code >> 1;
+        const uint32_t flip = ((code & 1) && f < t.Fi) ? 0x80000000u : 0u;  // sign flip as a bit
+        const R* fp = fflux + static_cast<size_t>(code < 0 ? 0 : f) * 5;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) bits[s][k] = code < 0 ? 0u : (__float_as_uint(fp[k]) ^ flip);
+      }
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        const uint32_t u[kMaxCellFaces] = {bits[0][k], bits[1][k], bits[2][k], bits[3][k], bits[4][k], bits[5][k]};
+        bool exact = true;
+        acc[k] = exact_sum_f32(u, exact);
+        if (!exact) {  // rare: a value far below the largest, or not finite
+          double a = 0.0;
+#pragma unroll
+          for (int s = 0; s < kMaxCellFaces; ++s) a += widen_exact(__uint_as_float(u[s]));
+          acc[k] = a;
+        }
+      }
+    }
+  }
 #pragma unroll
   for (int s = 0; s < kMaxCellFaces; ++s) {
+    if (std::is_same<R, float>::value && !cell_flux) break;  // summed above
     const int code = t.csr_flux[s * C + c];
     if (code < 0) continue;
     const int f = code >> 1;
@@ -723,8 +759,6 @@ __device__ __forceinline__ void residual_cell(const TopoView& t, const R* __rest
       const double v = negate_if(to_double<R>(fp[k]), neg);  // sign flip on the integer pipe
       if (cell_flux) {
         acc[k] = acc[k] + dtv * v;
-      } else if (std::is_same<R, float>::value && s == 0) {
-        acc[k] = v;  // the mixed form starts from its first term
       } else {
         acc[k] += v;  // the plain form adds to +0 as the reference does
       }
@@ -799,7 +833,7 @@ __global__ void __launch_bounds__(kFaceBlock) k_bc_flux(TopoView t, GeomView<R> 
 }
 
 template <class R>
-__global__ void __launch_bounds__(kCellBlock) k_residual(TopoView t, const R* __restrict__ fflux,
+__global__ void __launch_bounds__(kCellBlock, kResidualMinBlocks<R>) k_residual(TopoView t, const R* __restrict__ fflux,
                                                          double* __restrict__ Un, double* __restrict__ Unp1,
                                                          R* __restrict__ W, double* __restrict__ res_out, double dt,
                                                          int stage, bool cell_flux) {
@@ -863,6 +897,159 @@ __global__ void __launch_bounds__(256) kb_residual(const Segment<R>* __restrict_
     if (c < sg.t.C)
       residual_cell<R>(sg.t, sg.b.fflux, sg.s.Un, sg.s.Unp1, sg.b.W, sg.s.res, sg.dt, stage, cell_flux, c);
   }
+}
+
+// ---- one launch for whole batch steps: phases separated by a grid barrier ----
+// The batch's kernels of one RK stage become phases of one persistent
+// kernel: (A) Green-Gauss/limiter sweep and boundary-face flux, (B)
+// internal-face flux, (C) residual and RK4 update; a grid-wide barrier
+// separates the phases and the stages, so a whole ma_batch_step is one
+// launch. It is launched cooperatively (all blocks resident, checked by the
+// runtime at launch), so every barrier completes; each wait is still bounded
+// (kGridBarrierTimeoutNs): a block that waits longer sets *err, every block
+// then leaves at its next barrier, and the host reports the error. Every
+// item is computed by the device functions of the per-kind kernels, so the
+// bits are the same.
+constexpr unsigned long long kGridBarrierTimeoutNs = 5000000000ull;  // 5 s
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Sense by generation: the last block to arrive resets the count and bumps
+// the generation; the others wait for the bump. Returns false when the
+// barrier gave up (timeout here or in another block).
+__device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned* gen, int* err) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* vgen = gen;
+    volatile int* verr = err;
+    const unsigned g = *vgen;
+    __threadfence();
+    int ok = *verr == 0;
+    if (atomicAdd(count, 1u) + 1u == gridDim.x) {
+      atomicExch(count, 0u);
+      __threadfence();
+      atomicAdd(gen, 1u);
+    } else {
+      const unsigned long long t0 = global_ns();
+      while (ok && *vgen == g) {
+        __nanosleep(64);
+        if (*verr != 0) ok = 0;
+        else if (global_ns() - t0 > kGridBarrierTimeoutNs) {
+          atomicExch(err, 1);
+          ok = 0;
+        }
+      }
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+struct GridSync {
+  unsigned* count;
+  unsigned* gen;
+  int* err;
+};
+
+template <class R, int MODE, bool SECOND, bool VISC>
+__global__ void __launch_bounds__(256) kb_steps(const Segment<R>* segs, const int2* c_sweep, const int2* c_flux,
+                                                const int2* c_bc, const int2* c_res, const int* nchunks, Transport tr,
+                                                bool has_sweep, bool cell_flux, int nsteps, GridSync gs) {
+  const int n0 = nchunks[0], n1 = nchunks[1], n2 = nchunks[2], n3 = nchunks[3];
+  for (int step = 0; step < nsteps; ++step) {
+    for (int stage = 0; stage < 4; ++stage) {
+      if (has_sweep) {
+        for (int ch = blockIdx.x; ch < n0; ch += gridDim.x) {
+          const int2 cs = c_sweep[ch];
+          const Segment<R>& sg = segs[cs.x];
+          const int c = cs.y + threadIdx.x;
+          if constexpr (kWarpVenkat<R, MODE, true>) {
+            sweep1_cell<R, MODE, true>(sg.t, sg.g, sg.b.W, sg.b.grad, sg.b.phi, c < sg.t.C ? c : sg.t.C - 1,
+                                       c < sg.t.C);
+          } else if (c < sg.t.C) {
+            sweep1_cell<R, MODE>(sg.t, sg.g, sg.b.W, sg.b.grad, sg.b.phi, c);
+          }
+        }
+      }
+      for (int ch = blockIdx.x; ch < n2; ch += gridDim.x) {
+        const int2 cs = c_bc[ch];
+        const Segment<R>& sg = segs[cs.x];
+        const int i = cs.y + threadIdx.x;
+        if (i < sg.t.Fb) bc_flux_face<R>(sg.t, sg.g, sg.b.W, tr, sg.inflow, sg.b.fflux, i);
+      }
+      // The internal-face flux reads the sweep's gradients and limiter; with
+      // no sweep it shares the first phase.
+      if (has_sweep && !grid_barrier(gs.count, gs.gen, gs.err)) return;
+      for (int ch = blockIdx.x; ch < n1; ch += gridDim.x) {
+        const int2 cs = c_flux[ch];
+        const Segment<R>& sg = segs[cs.x];
+        const int f = cs.y + threadIdx.x;
+        if (f < sg.t.Fi)
+          internal_flux_face<R, SECOND, VISC>(sg.t, sg.g, sg.b.W, sg.b.grad, sg.b.phi, tr, sg.b.fflux, f);
+      }
+      if (!grid_barrier(gs.count, gs.gen, gs.err)) return;
+      for (int ch = blockIdx.x; ch < n3; ch += gridDim.x) {
+        const int2 cs = c_res[ch];
+        const Segment<R>& sg = segs[cs.x];
+        const int c = cs.y + threadIdx.x;
+        if (c < sg.t.C)
+          residual_cell<R>(sg.t, sg.b.fflux, sg.s.Un, sg.s.Unp1, sg.b.W, sg.s.res, sg.dt, stage, cell_flux, c);
+      }
+      const bool last = step == nsteps - 1 && stage == 3;
+      if (!last && !grid_barrier(gs.count, gs.gen, gs.err)) return;
+    }
+  }
+}
+
+template <class R>
+cudaError_t launch_batch_steps_impl(const PathConfig& cfg, const Segment<R>* segs, const BatchLaunch& bl,
+                                    int nsteps, unsigned* barrier_words, int* err, int block, int grid,
+                                    cudaStream_t stream) {
+  const Transport tr = cfg.transport;
+  const bool has_sweep = cfg.second_order || cfg.viscous;
+  const int mode = !cfg.second_order ? 0 : (cfg.limiter == 1 ? 2 : 1);
+  GridSync gs{barrier_words, barrier_words + 1, err};
+  const int2* c0 = bl.chunks[0];
+  const int2* c1 = bl.chunks[1];
+  const int2* c2 = bl.chunks[2];
+  const int2* c3 = bl.chunks[3];
+  const int* nc = bl.nchunks;
+  bool cf = cfg.cell_flux;
+  void* args[] = {(void*)&segs, (void*)&c0, (void*)&c1, (void*)&c2, (void*)&c3, (void*)&nc, (void*)&tr,
+                  (void*)&has_sweep, (void*)&cf, (void*)&nsteps, (void*)&gs};
+  const void* fn = nullptr;
+  if (mode == 0) {
+    fn = cfg.viscous ? (const void*)kb_steps<R, 0, false, true> : (const void*)kb_steps<R, 0, false, false>;
+  } else if (mode == 1) {
+    fn = cfg.viscous ? (const void*)kb_steps<R, 1, true, true> : (const void*)kb_steps<R, 1, true, false>;
+  } else {
+    fn = cfg.viscous ? (const void*)kb_steps<R, 2, true, true> : (const void*)kb_steps<R, 2, true, false>;
+  }
+  const size_t smem = (mode == 1 && std::is_same<R, double>::value) ? block / 32 * kVenkatBufBytes : 0;
+  return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(block), args, smem, stream);
+}
+
+// Resident blocks per SM of the single-launch kernel for this configuration.
+template <class R>
+cudaError_t batch_steps_occupancy_impl(const PathConfig& cfg, int block, int* blocks_per_sm) {
+  const int mode = !cfg.second_order ? 0 : (cfg.limiter == 1 ? 2 : 1);
+  const void* fn = nullptr;
+  if (mode == 0) {
+    fn = cfg.viscous ? (const void*)kb_steps<R, 0, false, true> : (const void*)kb_steps<R, 0, false, false>;
+  } else if (mode == 1) {
+    fn = cfg.viscous ? (const void*)kb_steps<R, 1, true, true> : (const void*)kb_steps<R, 1, true, false>;
+  } else {
+    fn = cfg.viscous ? (const void*)kb_steps<R, 2, true, true> : (const void*)kb_steps<R, 2, true, false>;
+  }
+  const size_t smem = (mode == 1 && std::is_same<R, double>::value) ? block / 32 * kVenkatBufBytes : 0;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, block, smem);
 }
 
 // Primitives of U_n + 0 * res with res = 0 (first stage after set_state).

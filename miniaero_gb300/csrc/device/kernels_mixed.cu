@@ -27,5 +27,15 @@ cudaError_t launch_batch_stage<float>(const PathConfig& cfg, const Segment<float
   return launch_batch_stage_impl<float>(cfg, segs, bl, stage, stream, kernels);
 }
 
+cudaError_t launch_batch_steps_mixed(const PathConfig& cfg, const void* segs, const BatchLaunch& bl, int nsteps,
+                               unsigned* barrier_words, int* err, int block, int grid, cudaStream_t stream) {
+  return launch_batch_steps_impl<float>(cfg, static_cast<const Segment<float>*>(segs), bl, nsteps, barrier_words, err,
+                                     block, grid, stream);
+}
+
+cudaError_t batch_steps_occupancy_mixed(const PathConfig& cfg, int block, int* blocks_per_sm) {
+  return batch_steps_occupancy_impl<float>(cfg, block, blocks_per_sm);
+}
+
 }  // namespace dev
 }  // namespace miniaero

@@ -108,6 +108,41 @@ __device__ __forceinline__ float narrow_rn(double x) {
   return __double2float_rn(x);
 }
 
+// Sum of six FP32 values (bit patterns) as the exact sum rounded once to
+// FP64: never less accurate than adding them in FP64 one after another, and
+// done on the integer pipe. Each value's 24-bit significand is placed in a
+// 64-bit fixed-point word 36 bits above the binade of the largest value
+// (six such words stay below 2^63), the words are summed exactly, and the
+// integer is converted once (round to nearest even) and scaled by a power of
+// two through the exponent field. Zeros and FP32 subnormals add nothing (the
+// mixed form's widening also takes subnormals as zero). `exact` becomes false
+// when a nonzero value lies more than 36 binades below the largest, or a value
+// is infinite or NaN; the caller then adds in FP64.
+__device__ __forceinline__ double exact_sum_f32(const uint32_t (&u)[6], bool& exact) {
+  uint32_t emax = 0;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) emax = max(emax, (u[i] >> 23) & 0xFFu);
+  bool ok = emax < 255u;
+  long long acc = 0;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    const uint32_t e = (u[i] >> 23) & 0xFFu;
+    const uint32_t d = emax - e;
+    const bool live = e != 0u;
+    const bool fits = d <= 36u;
+    ok &= !live | fits;
+    const long long m = static_cast<long long>((u[i] & 0x7FFFFFu) | 0x800000u);
+    const long long a = (live & fits) ? (m << (36u - d)) : 0LL;
+    acc += (u[i] >> 31) ? -a : a;
+  }
+  exact = ok;
+  if (acc == 0) return 0.0;
+  // acc * 2^(emax - 150 - 36): the exponent field of the converted integer
+  // (at least 1 in magnitude) is raised by emax - 186 >= -185, still normal.
+  const double r = static_cast<double>(acc);
+  return __longlong_as_double(__double_as_longlong(r) + (static_cast<long long>(emax) - 186LL) * (1LL << 52));
+}
+
 // -x when neg, by flipping the sign bit on the integer pipe (IEEE negation).
 __device__ __forceinline__ double negate_if(double x, bool neg) {
   return __longlong_as_double(__double_as_longlong(x) ^ (static_cast<long long>(neg) << 63));

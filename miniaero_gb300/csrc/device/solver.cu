@@ -70,6 +70,7 @@ struct ma_solver {
   ma_options opts;
   dev::PathConfig cfg;
   bool mixed = false;
+  bool fma = false;  // MA_PREC_FP64_FMA: the FP64 kernels built with multiply-add contraction
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;       // graph side branch: the boundary-face flux
   cudaEvent_t fork = nullptr, join = nullptr;
@@ -554,6 +555,13 @@ extern "C" size_t ma_mesh_device_bytes(const ma_mesh* m) { return m ? m->bytes :
 // ---------------------------------------------------------------------------
 namespace {
 
+// One stage's kernels (those in `kernels`) in the solver's precision.
+cudaError_t solver_stage(ma_solver* s, int stage, cudaStream_t stream, unsigned kernels) {
+  if (s->mixed) return dev::launch_stage<float>(s->topo, s->mesh->g32, s->cfg, s->st, s->b32, stage, stream, kernels);
+  if (s->fma) return dev::launch_stage_fma(s->topo, s->mesh->g64, s->cfg, s->st, s->b64, stage, stream, kernels);
+  return dev::launch_stage<double>(s->topo, s->mesh->g64, s->cfg, s->st, s->b64, stage, stream, kernels);
+}
+
 ma_status capture_step_graph(ma_solver* s) {
   if (s->graph) {
     cudaGraphExecDestroy(s->graph);
@@ -563,11 +571,7 @@ ma_status capture_step_graph(ma_solver* s) {
   MA_CUDA_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   cudaError_t e = cudaSuccess;
   for (int stage = 0; stage < 4 && e == cudaSuccess; ++stage) {
-    auto launch = [&](cudaStream_t stream, unsigned kernels) {
-      return s->mixed
-                 ? dev::launch_stage<float>(s->topo, s->mesh->g32, s->cfg, s->st, s->b32, stage, stream, kernels)
-                 : dev::launch_stage<double>(s->topo, s->mesh->g64, s->cfg, s->st, s->b64, stage, stream, kernels);
-    };
+    auto launch = [&](cudaStream_t stream, unsigned kernels) { return solver_stage(s, stage, stream, kernels); };
     // The boundary-face flux reads only the stage's primitives and writes its
     // own flux slots: a side branch of the graph runs it beside the sweep and
     // the internal-face flux, and the residual waits for both branches.
@@ -598,7 +602,8 @@ ma_status capture_step_graph(ma_solver* s) {
 extern "C" ma_status ma_solver_create(ma_mesh* mesh, const ma_options* o, ma_solver** out) {
   if (!mesh || !o || !out) return set_error(MA_EINVAL, "ma_solver_create: null argument");
   *out = nullptr;
-  if (o->precision != MA_PREC_FP64 && o->precision != MA_PREC_MIXED) return set_error(MA_EINVAL, "bad precision");
+  if (o->precision != MA_PREC_FP64 && o->precision != MA_PREC_MIXED && o->precision != MA_PREC_FP64_FMA)
+    return set_error(MA_EINVAL, "bad precision");
   if (o->limiter != MA_LIMITER_VENKAT && o->limiter != MA_LIMITER_VANALBADA) return set_error(MA_EINVAL, "bad limiter");
   if (o->viscosity_model != MA_VISC_SUTHERLAND && o->viscosity_model != MA_VISC_CONSTANT)
     return set_error(MA_EINVAL, "bad viscosity model");
@@ -615,6 +620,7 @@ extern "C" ma_status ma_solver_create(ma_mesh* mesh, const ma_options* o, ma_sol
   s->cfg.cell_flux = o->gather == MA_GATHER_CELL_FLUX;
   s->opts = *o;
   s->mixed = o->precision == MA_PREC_MIXED;
+  s->fma = o->precision == MA_PREC_FP64_FMA;
   s->cfg.second_order = o->second_order_space != 0;
   s->cfg.viscous = o->viscous != 0;
   s->cfg.limiter = o->limiter;
@@ -741,6 +747,8 @@ extern "C" ma_status ma_solver_set_state(ma_solver* s, const double* U, int32_t 
   }
   if (s->mixed)
     MA_CUDA_TRY(dev::launch_init_primitives<float>(t, s->st, s->b32, s->stream));
+  else if (s->fma)
+    MA_CUDA_TRY(dev::launch_init_primitives_fma(t, s->st, s->b64, s->stream));
   else
     MA_CUDA_TRY(dev::launch_init_primitives<double>(t, s->st, s->b64, s->stream));
   if (s->st.res) MA_CUDA_TRY(cudaMemsetAsync(s->st.res, 0, sizeof(double) * 5 * t.C, s->stream));
@@ -814,8 +822,7 @@ extern "C" ma_status ma_solver_profile_steps(ma_solver* s, int32_t nsteps, doubl
         ev.push_back(b);
         kind.push_back(k);
         cudaEventRecord(a, s->stream);
-        cudaError_t e = s->mixed ? dev::launch_stage<float>(t, s->mesh->g32, s->cfg, s->st, s->b32, stage, s->stream, bits[k])
-                                 : dev::launch_stage<double>(t, s->mesh->g64, s->cfg, s->st, s->b64, stage, s->stream, bits[k]);
+        cudaError_t e = solver_stage(s, stage, s->stream, bits[k]);
         cudaEventRecord(b, s->stream);
         if (e != cudaSuccess) {
           cleanup();

@@ -90,6 +90,7 @@ extern "C" ma_status ma_options_read(const char* path, ma_options* o) {
       std::string v; in >> v;
       if (v == "fp64") o->precision = MA_PREC_FP64;
       else if (v == "mixed") o->precision = MA_PREC_MIXED;
+      else if (v == "fp64_fma") o->precision = MA_PREC_FP64_FMA;
       else ok = false;
     } else if (key == "cfl") {
       in >> o->cfl;

@@ -136,3 +136,56 @@ def test_batch_profile_steps_equal_graph_steps(has_gpu):
         b.close()
     for a, c in zip(*out):
         assert np.array_equal(a, c)
+
+
+@pytest.mark.parametrize("precision,second,viscous,limiter", [
+    (ma.MA_PREC_FP64, 1, 1, ma.MA_LIMITER_VENKAT), (ma.MA_PREC_MIXED, 1, 1, ma.MA_LIMITER_VENKAT),
+    (ma.MA_PREC_FP64, 1, 1, ma.MA_LIMITER_VANALBADA), (ma.MA_PREC_FP64, 0, 0, ma.MA_LIMITER_VENKAT),
+    (ma.MA_PREC_FP64_FMA, 1, 1, ma.MA_LIMITER_VENKAT)])
+def test_single_launch_steps_equal_single_solves(has_gpu, precision, second, viscous, limiter):
+    """ma_batch_set_single_launch: a whole ma_batch_step (several RK4 steps,
+    every member) as one cooperative launch gives each member the bits of
+    its solve alone, for uneven members, across calls and after membership
+    changes."""
+    o = sod_options(precision, second, viscous)
+    o.limiter = limiter
+
+    def same(a, ref):
+        if precision != ma.MA_PREC_FP64_FMA:
+            return np.array_equal(a, ref)
+        # The contracted form is compiled per kernel; fused operations may be
+        # chosen differently in the one-launch kernel than in the per-kind ones.
+        scale = np.abs(ref).max(axis=0)
+        scale[1:4] = scale[1:4].max()
+        return bool(np.all(np.abs(a - ref).max(axis=0) <= 1e-11 * scale))
+
+    dims = [(12, 6, 4), (20, 3, 5), (7, 7, 7), (33, 9, 5), (1, 1, 1), (48, 16, 16)]
+    rng = np.random.default_rng(1)
+    cases = [member(o, d, rng.uniform(2, 20), rng.uniform(2, 20)) for d in dims]
+    b = ma.Batch(o, capacity=16, budget_bytes=1 << 30)
+    grid = b.set_single_launch(256)
+    assert grid >= 152
+    meshes = [ma.DeviceMesh(md) for _, md, _ in cases]
+    ids = [b.add(dm, U0) for dm, (_, _, U0) in zip(meshes, cases)]
+    b.step(5)
+    b.step(2)
+    b.synchronize()
+    for (m, md, U0), i in zip(cases, ids):
+        assert same(b.get_state(i), single(md, m, U0, 7, b.member_dt(i)))
+    # A member leaves and another joins: the next single launch covers the new set.
+    b.remove(ids[2])
+    extra = member(o, (9, 11, 3), 5.0, 7.0)
+    dx = ma.DeviceMesh(extra[1])
+    ix = b.add(dx, extra[2])
+    b.step(3)
+    b.synchronize()
+    assert same(b.get_state(ix), single(extra[1], extra[0], extra[2], 3, b.member_dt(ix)))
+    assert same(b.get_state(ids[0]), single(cases[0][1], cases[0][0], cases[0][2], 10, b.member_dt(ids[0])))
+    # Back to per-kind launches: same bits.
+    b.set_single_launch(0)
+    b.step(1)
+    b.synchronize()
+    assert same(b.get_state(ix), single(extra[1], extra[0], extra[2], 4, b.member_dt(ix)))
+    b.close()
+    for dm in meshes + [dx]:
+        dm.close()

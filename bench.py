@@ -486,7 +486,7 @@ def one_launch_value(ma, name, steps, warmup):
         dm = ma.DeviceMesh(md)
         b = ma.Batch(o, capacity=1, budget_bytes=64 << 30)
         grid = b.set_single_launch(256)
-        b.add(dm, U0)
+        b.add(dm, U0, dt=(o.dt if not o.cfl > 0 else 0.0))
         b.step(warmup)
         b.synchronize()
         stream = torch.cuda.ExternalStream(b.stream)
@@ -834,7 +834,8 @@ def serving_physics(ma):
                       cfl=0.5)
 
 
-def run_serving(ma, reqs, static, budget=150 << 30, tick=25, max_running_cells=8_000_000, nsteps=SERVE_STEPS):
+def run_serving(ma, reqs, static, budget=150 << 30, tick=25, max_running_cells=8_000_000, nsteps=SERVE_STEPS,
+                preload=True):
     """Serves the requests (arrival offset s, n, Mach) through ma.Server:
     admitted under the HBM budget with at most max_running_cells cells
     running at once (the latency control: it bounds how many requests share
@@ -846,8 +847,9 @@ def run_serving(ma, reqs, static, budget=150 << 30, tick=25, max_running_cells=8
     srv.set_max_running_cells(max_running_cells)
     srv.set_launch(*static["launch"])
     t0 = time.perf_counter()
-    for n in sorted({n for _, n, _ in reqs}):  # mesh cache warm-up: one device mesh per size
-        srv.preload(ma.Server.request(n, n, n, 2.0, 0.5, 0.5, flat_plate_inflow(0.3), nsteps))
+    if preload:
+        for n in sorted({n for _, n, _ in reqs}):  # mesh cache warm-up: one device mesh per size
+            srv.preload(ma.Server.request(n, n, n, 2.0, 0.5, 0.5, flat_plate_inflow(0.3), nsteps))
     setup_s = time.perf_counter() - t0
     ids = []
     start = time.perf_counter()
@@ -904,8 +906,16 @@ def run_serving_suite(ma, n_requests=32, rate=200.0, loads=(0.25, 0.5, 0.9), n_l
         out["load_%d_pct" % round(load * 100)] = dict(
             run_serving(ma, serving_requests(ma, n_load_requests, r), static, budget=budget),
             arrival_rate_per_s=r, target_load_of_static_batch=load)
+    # The 50 % load again with an empty mesh cache: every first request of a
+    # size waits for its mesh, built by the server's mesh thread while the
+    # running requests keep stepping.
+    r = 0.5 * static["value"] * 1e6 / mean_work
+    out["load_50_pct_uncached_meshes"] = dict(
+        run_serving(ma, serving_requests(ma, n_load_requests, r), static, budget=budget, preload=False),
+        arrival_rate_per_s=r, target_load_of_static_batch=0.5)
     summ = {}
-    for key in ["saturating_200_per_s"] + ["load_%d_pct" % round(x * 100) for x in loads]:
+    for key in (["saturating_200_per_s"] + ["load_%d_pct" % round(x * 100) for x in loads]
+                + ["load_50_pct_uncached_meshes"]):
         v = out[key]
         summ[key] = {"thru": _r(v["throughput"]["value"]), "p50_s": _r(v["latency_s"]["p50"], 3),
                      "p99_s": _r(v["latency_s"]["p99"], 3), "vs_batched": _r(v["serving_vs_batched"], 3)}

@@ -8,7 +8,11 @@
 // length and the fewest steps any running request has left), so requests
 // finish exactly on their step count and new arrivals join at the next tick.
 // A scheduler thread drives the loop (or the caller does, through
-// ma_server_poll). In dry-run mode no device call is made: member and mesh
+// ma_server_poll). With the scheduler thread, a mesh shape not yet cached is
+// built (host mesh and device upload) by a second thread, started when the
+// request is submitted: the running requests keep stepping meanwhile, and the
+// request waits at the head of the queue only if its mesh is not ready when
+// its turn comes. In dry-run mode no device call is made: member and mesh
 // sizes come from the mesh dimensions and ticks only advance counters, which
 // is how the admission logic is tested without a GPU.
 #include <algorithm>
@@ -22,6 +26,8 @@
 #include <thread>
 #include <tuple>
 #include <vector>
+
+#include <cuda_runtime_api.h>
 
 #include "../../../include/miniaero_gpu.h"
 #include "trace.hpp"
@@ -100,6 +106,14 @@ struct ma_server {
   int64_t running_cells = 0;
   ma_server_stats stats;
   int64_t busy_start = -1;
+  // Mesh builds off the scheduler thread (thread mode, not dry-run).
+  bool async_meshes = false;
+  int device = 0;
+  std::thread mesher;
+  std::condition_variable mesh_cv;                  // a build job is waiting
+  std::deque<MeshKey> mesh_jobs;
+  std::map<MeshKey, std::pair<ma_options, size_t>> building;  // options, bytes reserved in `used`
+  std::map<MeshKey, std::pair<ma_status, std::string>> failed_meshes;
 };
 
 namespace {
@@ -201,6 +215,65 @@ void release_member(ma_server* s, Request& q) {
   if (it != s->meshes.end()) it->second.users--;
 }
 
+// Queues a build of the request's mesh on the mesh thread unless it is
+// cached or already being built, reserving its device bytes (an upper bound)
+// in the budget; may_evict lets unused cached meshes go to make room.
+// Returns whether the mesh is cached, building or now queued. Called with mu
+// held.
+bool start_mesh_build(ma_server* s, const Request& q, bool may_evict) {
+  if (s->meshes.count(q.key) || s->building.count(q.key)) return true;
+  const size_t need = dry_mesh_bytes(s, q.req);
+  if (may_evict ? !make_room(s, need) : s->used + need > s->budget) return false;
+  s->used += need;
+  s->building[q.key] = std::make_pair(options_of(s, q.req), need);
+  s->mesh_jobs.push_back(q.key);
+  s->mesh_cv.notify_one();
+  return true;
+}
+
+void mesher_loop(ma_server* s) {
+  cudaSetDevice(s->device);
+  std::unique_lock<std::mutex> lk(s->mu);
+  for (;;) {
+    s->mesh_cv.wait(lk, [&]() { return s->stop || !s->mesh_jobs.empty(); });
+    if (s->stop) return;
+    const MeshKey key = s->mesh_jobs.front();
+    s->mesh_jobs.pop_front();
+    const ma_options o = s->building[key].first;
+    lk.unlock();
+    CachedMesh cm;
+    ma_status st;
+    std::string msg;
+    {
+      miniaero::TraceRange trace("ma_server_mesh_build");
+      st = ma_host_mesh_build(&o, &cm.host);
+      if (st == MA_OK) {
+        ma_mesh_view v;
+        ma_host_mesh_view(cm.host, &v);
+        st = ma_mesh_upload_ex(&v, s->physics.gather == MA_GATHER_CELL_FLUX ? MA_MESH_CELL_FLUX : 0, &cm.dev);
+        if (st != MA_OK) {
+          msg = ma_last_error();
+          ma_host_mesh_free(cm.host);
+        }
+      } else {
+        msg = ma_last_error();
+      }
+    }
+    lk.lock();
+    s->used -= s->building[key].second;
+    s->building.erase(key);
+    if (st == MA_OK) {
+      cm.bytes = ma_mesh_device_bytes(cm.dev);
+      cm.last_used = ns_since(s->t0);
+      s->used += cm.bytes;
+      s->meshes.emplace(key, cm);
+    } else {
+      s->failed_meshes[key] = std::make_pair(st, msg);
+    }
+    s->cv.notify_all();
+  }
+}
+
 // Admits queued requests in order while they fit. Called with mu held.
 void admit(ma_server* s) {
   while (!s->queue.empty()) {
@@ -218,6 +291,21 @@ void admit(ma_server* s) {
       if (s->max_running_cells > 0 && s->running_cells > 0 && s->running_cells + C > s->max_running_cells) return;
     }
     const bool cached = s->meshes.count(q.key) != 0;
+    if (!cached && s->async_meshes) {
+      auto failed = s->failed_meshes.find(q.key);
+      if (failed != s->failed_meshes.end()) {
+        q.error = failed->second.first;
+        q.message = failed->second.second;
+        s->failed_meshes.erase(failed);
+        s->queue.pop_front();
+        finish(s, q, MA_REQ_FAILED);
+        continue;
+      }
+      // The head of the queue waits for its mesh (the mesh thread builds it);
+      // the running requests keep stepping meanwhile.
+      start_mesh_build(s, q, true);
+      return;
+    }
     const size_t mesh_need = cached ? 0 : dry_mesh_bytes(s, q.req);
     size_t member_need = dry_member_bytes(s, q.req);
     if (!make_room(s, mesh_need + member_need)) return;  // wait for memory
@@ -384,7 +472,14 @@ extern "C" ma_status ma_server_create(const ma_options* physics, size_t budget_b
       return st;
     }
   }
-  if (flags & MA_SERVER_THREAD) s->worker = std::thread(worker_loop, s);
+  if (flags & MA_SERVER_THREAD) {
+    if (!s->dry) {
+      cudaGetDevice(&s->device);
+      s->async_meshes = true;
+      s->mesher = std::thread(mesher_loop, s);
+    }
+    s->worker = std::thread(worker_loop, s);
+  }
   *out = s;
   return MA_OK;
 }
@@ -396,7 +491,9 @@ extern "C" void ma_server_free(ma_server* s) {
     s->stop = true;
   }
   s->cv.notify_all();
+  s->mesh_cv.notify_all();
   if (s->worker.joinable()) s->worker.join();
+  if (s->mesher.joinable()) s->mesher.join();
   if (s->batch) ma_batch_free(s->batch);
   for (auto& kv : s->meshes) {
     if (kv.second.dev) ma_mesh_free(kv.second.dev);
@@ -456,6 +553,9 @@ extern "C" ma_status ma_server_submit(ma_server* s, const ma_request* r, int64_t
     s->stats.failed++;
   } else {
     s->queue.push_back(q.id);
+    // Start building an uncached mesh now, while the request waits its turn
+    // (only into free budget: evicting is left to admission).
+    if (s->async_meshes) start_mesh_build(s, q, false);
   }
   s->stats.submitted++;
   *id = q.id;

@@ -474,9 +474,19 @@ def measure_config(ma, args, world, rank, local, name, err_steps, timed_steps, c
     return res
 
 
-def one_launch_value(ma, name, steps, warmup):
+def one_launch_value(ma, name, steps, warmup, blocks=(128, 256)):
     """The configuration as a one-member batch in single-launch mode: all
-    `steps` RK4 steps in one cooperative launch (no per-kernel launches)."""
+    `steps` RK4 steps in one cooperative launch (no per-kernel launches), at
+    each block size in `blocks`; the faster is reported."""
+    out = {}
+    for block in blocks:
+        for prec_name, r in _one_launch(ma, name, steps, warmup, block).items():
+            if prec_name not in out or r["value"] > out[prec_name]["value"]:
+                out[prec_name] = dict(r, tried_blocks=list(blocks))
+    return out
+
+
+def _one_launch(ma, name, steps, warmup, block):
     import torch
     out = {}
     for prec_name in ("fp64", "mixed"):
@@ -485,7 +495,7 @@ def one_launch_value(ma, name, steps, warmup):
         U0 = ma.initial_state(md, o)
         dm = ma.DeviceMesh(md)
         b = ma.Batch(o, capacity=1, budget_bytes=64 << 30)
-        grid = b.set_single_launch(256)
+        grid = b.set_single_launch(block)
         b.add(dm, U0, dt=(o.dt if not o.cfl > 0 else 0.0))
         b.step(warmup)
         b.synchronize()
@@ -497,7 +507,7 @@ def one_launch_value(ma, name, steps, warmup):
         b.synchronize()
         ms = e0.elapsed_time(e1)
         out[prec_name] = {"value": md.ncells * 4 * steps / (ms / 1e3) / 1e6, "unit": "Mcell-stage/s",
-                          "steps": steps, "launches": 1, "block": 256, "grid": grid}
+                          "steps": steps, "launches": 1, "block": block, "grid": grid}
         b.close()
         dm.close()
     return out

@@ -42,7 +42,7 @@ constexpr int kFluxMinBlocks = std::is_same<R, float>::value ? 8 : 0;
 // Resident residual blocks per SM (0: no bound). The mixed residual holds a
 // cell's 30 face-flux words for its integer sums.
 template <class R>
-constexpr int kResidualMinBlocks = std::is_same<R, float>::value ? 0 : 0;
+constexpr int kResidualMinBlocks = std::is_same<R, float>::value ? 6 : 0;
 
 // Primitives of an FP64 state written as R: FP64 arithmetic for the plain
 // form (bit-exact), FP32 for the mixed form (its flux work is FP32 anyway).
@@ -961,11 +961,14 @@ struct GridSync {
 template <class R, int MODE, bool SECOND, bool VISC>
 __global__ void __launch_bounds__(256) kb_steps(const Segment<R>* segs, const int2* c_sweep, const int2* c_flux,
                                                 const int2* c_bc, const int2* c_res, const int* nchunks, Transport tr,
-                                                bool has_sweep, bool cell_flux, int nsteps, GridSync gs) {
+                                                bool cell_flux, int nsteps, GridSync gs) {
+  // The sweep phase exists for second-order or viscous runs only; without it
+  // the kernel carries no sweep code (fewer registers, more resident blocks).
+  constexpr bool has_sweep = SECOND || VISC;
   const int n0 = nchunks[0], n1 = nchunks[1], n2 = nchunks[2], n3 = nchunks[3];
   for (int step = 0; step < nsteps; ++step) {
     for (int stage = 0; stage < 4; ++stage) {
-      if (has_sweep) {
+      if constexpr (has_sweep) {
         for (int ch = blockIdx.x; ch < n0; ch += gridDim.x) {
           const int2 cs = c_sweep[ch];
           const Segment<R>& sg = segs[cs.x];
@@ -1013,7 +1016,6 @@ cudaError_t launch_batch_steps_impl(const PathConfig& cfg, const Segment<R>* seg
                                     int nsteps, unsigned* barrier_words, int* err, int block, int grid,
                                     cudaStream_t stream) {
   const Transport tr = cfg.transport;
-  const bool has_sweep = cfg.second_order || cfg.viscous;
   const int mode = !cfg.second_order ? 0 : (cfg.limiter == 1 ? 2 : 1);
   GridSync gs{barrier_words, barrier_words + 1, err};
   const int2* c0 = bl.chunks[0];
@@ -1023,7 +1025,7 @@ cudaError_t launch_batch_steps_impl(const PathConfig& cfg, const Segment<R>* seg
   const int* nc = bl.nchunks;
   bool cf = cfg.cell_flux;
   void* args[] = {(void*)&segs, (void*)&c0, (void*)&c1, (void*)&c2, (void*)&c3, (void*)&nc, (void*)&tr,
-                  (void*)&has_sweep, (void*)&cf, (void*)&nsteps, (void*)&gs};
+                  (void*)&cf, (void*)&nsteps, (void*)&gs};
   const void* fn = nullptr;
   if (mode == 0) {
     fn = cfg.viscous ? (const void*)kb_steps<R, 0, false, true> : (const void*)kb_steps<R, 0, false, false>;

@@ -114,7 +114,7 @@ __device__ __forceinline__ float narrow_rn(double x) {
 // 64-bit fixed-point word 36 bits above the binade of the largest value
 // (six such words stay below 2^63), the words are summed exactly, and the
 // integer is converted once (round to nearest even) and scaled by a power of
-// two through the exponent field. Zeros and FP32 subnormals add nothing (the
+// two, also on the integer pipe. Zeros and FP32 subnormals add nothing (the
 // mixed form's widening also takes subnormals as zero). `exact` becomes false
 // when a nonzero value lies more than 36 binades below the largest, or a value
 // is infinite or NaN; the caller then adds in FP64.
@@ -137,10 +137,20 @@ __device__ __forceinline__ double exact_sum_f32(const uint32_t (&u)[6], bool& ex
   }
   exact = ok;
   if (acc == 0) return 0.0;
-  // acc * 2^(emax - 150 - 36): the exponent field of the converted integer
-  // (at least 1 in magnitude) is raised by emax - 186 >= -185, still normal.
-  const double r = static_cast<double>(acc);
-  return __longlong_as_double(__double_as_longlong(r) + (static_cast<long long>(emax) - 186LL) * (1LL << 52));
+  // Integer-pipe conversion: normalise |acc| to bit 63, round to 53 bits
+  // (nearest even), assemble sign, exponent and fraction.
+  const unsigned long long neg = acc < 0 ? 1ull : 0ull;
+  const unsigned long long mag = neg ? static_cast<unsigned long long>(-acc) : static_cast<unsigned long long>(acc);
+  const int lz = __clzll(static_cast<long long>(mag));
+  const unsigned long long nrm = mag << lz;
+  unsigned long long frac = nrm >> 11;                 // 53 bits with the leading one
+  const unsigned long long rem = nrm & 0x7FFull;
+  frac += (rem > 0x400ull || (rem == 0x400ull && (frac & 1ull))) ? 1ull : 0ull;
+  // value = frac * 2^(63 - lz - 52) * 2^(emax - 186); frac may have carried to
+  // 2^53, which the exponent addition below absorbs.
+  const long long e = (1023LL + 63 - lz) + (static_cast<long long>(emax) - 186LL);
+  const unsigned long long bits = (neg << 63) + (static_cast<unsigned long long>(e) << 52) + (frac - (1ull << 52));
+  return __longlong_as_double(static_cast<long long>(bits));
 }
 
 // -x when neg, by flipping the sign bit on the integer pipe (IEEE negation).

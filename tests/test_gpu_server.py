@@ -81,3 +81,22 @@ def test_threaded_server_with_budget_pressure(has_gpu):
     for r in rids:
         assert np.array_equal(srv.result(r), ref)
     srv.close()
+
+
+def test_threaded_server_builds_new_meshes_beside_running_requests(has_gpu):
+    """With its scheduler thread the server builds each new mesh shape on a
+    mesh thread of its own: requests of five different sizes, submitted while
+    a first one runs, all finish with the bits of their solves alone."""
+    phys = physics(ma.MA_PREC_FP64)
+    srv = ma.Server(phys, budget_bytes=2 << 30, tick_steps=5, capacity=16, thread=True)
+    jobs = [(16, 0.3, 40), (10, 0.2, 15), (14, 0.45, 20), (18, 0.55, 10), (9, 0.1, 25), (12, 0.35, 5)]
+    rids = {jobs[0]: srv.submit(ma.Server.request(16, 16, 16, 2.0, 0.5, 0.5, inflow(0.3), 40, keep_result=True))}
+    for j in jobs[1:]:
+        rids[j] = srv.submit(ma.Server.request(j[0], j[0], j[0], 2.0, 0.5, 0.5, inflow(j[1]), j[2], keep_result=True))
+    for r in rids.values():
+        assert srv.wait(r, timeout=300.0).state == srv.DONE
+    st = srv.stats()
+    assert st["completed"] == len(jobs) and st["cached_meshes"] == len(jobs)
+    for j, r in rids.items():
+        assert np.array_equal(srv.result(r), alone(phys, j[0], j[1], j[2])[0]), j
+    srv.close()

@@ -916,6 +916,16 @@ def run_serving_suite(ma, n_requests=32, rate=200.0, loads=(0.25, 0.5, 0.9), n_l
         out["load_%d_pct" % round(load * 100)] = dict(
             run_serving(ma, serving_requests(ma, n_load_requests, r), static, budget=budget),
             arrival_rate_per_s=r, target_load_of_static_batch=load)
+    # Host mesh generation of the largest serving size, geometry on the host's
+    # threads and on the device (the server's mesh thread uses the device).
+    mo = ma.Options(problem_type=1, nx=128, ny=128, nz=128, lx=2.0, ly=0.5, lz=0.5)
+    times = {}
+    for dev in (False, True):
+        ma.Parallel3DMesh.from_options(mo).fill_mesh_data(device_geometry=dev)  # warm (module load)
+        t0 = time.perf_counter()
+        ma.Parallel3DMesh.from_options(mo).fill_mesh_data(device_geometry=dev)
+        times["device_geometry" if dev else "host_geometry"] = time.perf_counter() - t0
+    out["mesh_build_128_cubed_s"] = times
     # The 50 % load again with an empty mesh cache: every first request of a
     # size waits for its mesh, built by the server's mesh thread while the
     # running requests keep stepping.

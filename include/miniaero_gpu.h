@@ -174,6 +174,13 @@ ma_status ma_checkpoint_read(const char* path, ma_checkpoint_info* info, double*
  * Parallel3DMesh.h:173-449): builds cells, faces, BC sets and the face
  * iteration permutations on the host. */
 ma_status ma_host_mesh_build(const ma_options* o, ma_host_mesh** out);
+/* As ma_host_mesh_build; with MA_HOST_MESH_DEVICE_GEOMETRY the per-face
+ * geometry (kokkos/Face.C:37-98) and the cell volumes and centroids
+ * (MeshProcessor.C:130-171) are computed on the current CUDA device,
+ * bit-identical to the host path; face order, shuffle and BinSort stay on
+ * the host. MA_ECUDA if the device cannot be used. */
+enum { MA_HOST_MESH_DEVICE_GEOMETRY = 1 };
+ma_status ma_host_mesh_build_ex(const ma_options* o, int32_t flags, ma_host_mesh** out);
 ma_status ma_host_mesh_view(const ma_host_mesh* m, ma_mesh_view* view);
 void ma_host_mesh_free(ma_host_mesh* m);
 /* Initial state on the host (kokkos/Initial_Conditions.h:38-133), U in AOS. */

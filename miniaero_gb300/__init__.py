@@ -178,10 +178,13 @@ class Parallel3DMesh:
         m.options = options.copy()
         return m
 
-    def fill_mesh_data(self):
+    def fill_mesh_data(self, device_geometry=False):
+        """fillMeshData on the host; device_geometry=True computes the face
+        and cell geometry on the current CUDA device (same bits)."""
         L = lib()
         h = ctypes.c_void_p()
-        check(L.ma_host_mesh_build(ctypes.byref(self.options.c), ctypes.byref(h)))
+        flags = _lib.MA_HOST_MESH_DEVICE_GEOMETRY if device_geometry else 0
+        check(L.ma_host_mesh_build_ex(ctypes.byref(self.options.c), flags, ctypes.byref(h)))
         v = _lib.ma_mesh_view()
         check(L.ma_host_mesh_view(h, ctypes.byref(v)))
         C = v.ncells

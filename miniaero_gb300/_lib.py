@@ -14,6 +14,7 @@ MA_BC_EXTRAPOLATE, MA_BC_TANGENT, MA_BC_INFLOW, MA_BC_NOSLIP = range(4)
 MA_LIMITER_VENKAT, MA_LIMITER_VANALBADA = 0, 1
 MA_VISC_SUTHERLAND, MA_VISC_CONSTANT = 0, 1
 MA_PREC_FP64, MA_PREC_MIXED, MA_PREC_FP64_FMA = 0, 1, 2
+MA_HOST_MESH_DEVICE_GEOMETRY = 1
 MA_GATHER_ATOMICS, MA_GATHER_CELL_FLUX = 0, 1
 MA_MESH_CELL_FLUX = 1
 MA_LAYOUT_AOS, MA_LAYOUT_SOA = 0, 1
@@ -162,6 +163,7 @@ _SIGNATURES = {
     "ma_checkpoint_read": (c_int32, [ctypes.c_char_p, ctypes.POINTER(ma_checkpoint_info), P_f64, ctypes.c_int64,
                                      c_int32]),
     "ma_host_mesh_build": (c_int32, [ctypes.POINTER(ma_options), ctypes.POINTER(c_void_p)]),
+    "ma_host_mesh_build_ex": (c_int32, [ctypes.POINTER(ma_options), c_int32, ctypes.POINTER(c_void_p)]),
     "ma_host_mesh_view": (c_int32, [c_void_p, ctypes.POINTER(ma_mesh_view)]),
     "ma_host_mesh_free": (None, [c_void_p]),
     "ma_host_initial_state": (c_int32, [c_void_p, ctypes.POINTER(ma_options), P_f64]),

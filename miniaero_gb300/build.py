@@ -45,6 +45,8 @@ DEVICE_SOURCES = [
     ("device/solver.cu", ["--fmad=false"]),
     ("device/batch.cu", ["--fmad=false"]),
     ("device/noalloc.cu", ["--fmad=false"]),
+    # Mesh geometry on the device, bit-identical to the host generator.
+    ("device/geometry.cu", ["--fmad=false"]),
 ]
 HOST_SOURCES = ["host/mesh.cpp", "host/options.cpp", "host/host_api.cpp", "host/server.cpp", "host/checkpoint.cpp"]
 

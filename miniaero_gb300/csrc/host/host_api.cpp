@@ -1,5 +1,6 @@
 // Host-side C ABI: errors, host mesh, initial conditions.
 #include <cstring>
+#include <memory>
 #include <new>
 #include <string>
 #include <vector>
@@ -8,6 +9,7 @@
 #include "trace.hpp"
 #include "errors.hpp"
 #include "mesh.hpp"
+#include "../device/device_geometry.hpp"
 
 namespace miniaero {
 namespace {
@@ -46,8 +48,13 @@ extern "C" const char* ma_status_string(ma_status s) {
 }
 
 extern "C" ma_status ma_host_mesh_build(const ma_options* o, ma_host_mesh** out) {
+  return ma_host_mesh_build_ex(o, 0, out);
+}
+
+extern "C" ma_status ma_host_mesh_build_ex(const ma_options* o, int32_t flags, ma_host_mesh** out) {
   if (!o || !out) return set_error(MA_EINVAL, "ma_host_mesh_build: null argument");
   *out = nullptr;
+  if (flags & ~MA_HOST_MESH_DEVICE_GEOMETRY) return set_error(MA_EINVAL, "ma_host_mesh_build_ex: unknown flags");
   miniaero::TraceRange trace("ma_host_mesh_build");
   // The device arrays index a mesh with 32-bit arithmetic: refuse a box that
   // ma_mesh_upload would refuse before building it.
@@ -63,8 +70,21 @@ extern "C" ma_status ma_host_mesh_build(const ma_options* o, ma_host_mesh** out)
   for (int i = 0; i < 6; ++i) spec.bc_override[i] = o->bc_override[i];
   ma_host_mesh* m = new (std::nothrow) ma_host_mesh;
   if (!m) return set_error(MA_ENOMEM, "ma_host_mesh_build: out of host memory");
+  std::unique_ptr<miniaero::GeometryEngine> engine;
+  if (flags & MA_HOST_MESH_DEVICE_GEOMETRY) {
+    std::string why;
+    engine = miniaero::make_device_geometry(&why);
+    if (!engine) {
+      delete m;
+      return set_error(MA_ECUDA, "ma_host_mesh_build_ex: device geometry: " + why);
+    }
+  }
   try {
-    const std::string err = miniaero::build_box_mesh(spec, m->mesh);
+    const std::string err = miniaero::build_box_mesh(spec, m->mesh, engine.get());
+    if (!err.empty() && err.compare(0, 16, "device geometry:") == 0) {
+      delete m;
+      return set_error(MA_ECUDA, "ma_host_mesh_build_ex: " + err);
+    }
     if (!err.empty()) { delete m; return set_error(MA_EINVAL, "ma_host_mesh_build: " + err); }
   } catch (const std::bad_alloc&) {
     delete m;

@@ -225,8 +225,8 @@ struct RawFace {
   int32_t nodes[4];  // in the creating element's face order
 };
 
-void fill_face_set(HostFaceSet& fs, const std::vector<RawFace>& raw, const std::vector<int64_t>& ids,
-                   const std::vector<double>& xyz) {
+std::string fill_face_set(HostFaceSet& fs, const std::vector<RawFace>& raw, const std::vector<int64_t>& ids,
+                          const std::vector<double>& xyz, GeometryEngine* engine) {
   const size_t n = ids.size();
   fs.nfaces = static_cast<int32_t>(n);
   fs.conn.resize(n * 2);
@@ -235,6 +235,7 @@ void fill_face_set(HostFaceSet& fs, const std::vector<RawFace>& raw, const std::
   fs.normal.resize(n * 3);
   fs.tangent.resize(n * 3);
   fs.binormal.resize(n * 3);
+  std::vector<int32_t> nodes4(engine ? n * 4 : 0);
   // Faces come in shuffled order, so the node lookups are random: spread
   // them over the host's threads.
   parallel_for(n, [&](size_t b, size_t e) {
@@ -244,16 +245,26 @@ void fill_face_set(HostFaceSet& fs, const std::vector<RawFace>& raw, const std::
       fs.conn[2 * i + 1] = f.cv_plus;
       fs.flux_index[2 * i] = f.flux_minus;
       fs.flux_index[2 * i + 1] = f.flux_plus;
-      face_geometry(f.nodes, xyz, &fs.coords[3 * i], &fs.normal[3 * i], &fs.tangent[3 * i],
-                    &fs.binormal[3 * i]);
+      if (engine) {
+        for (int q = 0; q < 4; ++q) nodes4[4 * i + q] = f.nodes[q];
+      } else {
+        face_geometry(f.nodes, xyz, &fs.coords[3 * i], &fs.normal[3 * i], &fs.tangent[3 * i],
+                      &fs.binormal[3 * i]);
+      }
     }
   });
+  if (engine && n > 0) {
+    const std::string err = engine->faces(n, nodes4.data(), fs.coords.data(), fs.normal.data(), fs.tangent.data(),
+                                          fs.binormal.data());
+    if (!err.empty()) return err;
+  }
   fs.permutation = binsort_permutation(fs.conn.data(), fs.nfaces, 2);
+  return std::string();
 }
 
 }  // namespace
 
-std::string build_box_mesh(const MeshSpec& spec, HostMesh& out) {
+std::string build_box_mesh(const MeshSpec& spec, HostMesh& out, GeometryEngine* engine) {
   if (spec.nx < 1 || spec.ny < 1 || spec.nz < 1) return "mesh dimensions must be >= 1";
   const int64_t ncells64 = static_cast<int64_t>(spec.nx) * spec.ny * spec.nz;
   if (ncells64 > (1LL << 30)) return "mesh too large for 32-bit cell indices";
@@ -336,8 +347,18 @@ std::string build_box_mesh(const MeshSpec& spec, HostMesh& out) {
   out.ncells = ncells;
   out.cell_coords.resize(static_cast<size_t>(ncells) * 3);
   out.cell_volumes.resize(static_cast<size_t>(ncells));
+  if (engine) {
+    std::string err = engine->set_nodes(xyz.data(), static_cast<size_t>(nnodes));
+    int negative = 0;
+    if (err.empty())
+      err = engine->cells(static_cast<size_t>(ncells), conn.data(), out.cell_volumes.data(), out.cell_coords.data(),
+                          &negative);
+    if (!err.empty()) return "device geometry: " + err;
+    if (negative)
+      std::fprintf(stderr, "miniaero: warning: %d Gauss points with Jacobian determinant < 1e-300\n", negative);
+  }
   std::atomic<int> negative_total{0};
-  parallel_for(static_cast<size_t>(ncells), [&](size_t b, size_t e) {
+  if (!engine) parallel_for(static_cast<size_t>(ncells), [&](size_t b, size_t e) {
     int negative = 0;
     for (size_t ie = b; ie < e; ++ie) {
       const int32_t* en = &conn[ie * 8];
@@ -394,7 +415,10 @@ std::string build_box_mesh(const MeshSpec& spec, HostMesh& out) {
   GlibcRand rng(1);
   random_shuffle_glibc(internal_ids, rng);
 
-  fill_face_set(out.internal, raw, internal_ids, xyz);
+  {
+    const std::string err = fill_face_set(out.internal, raw, internal_ids, xyz, engine);
+    if (!err.empty()) return "device geometry: " + err;
+  }
   out.internal.name = "internal";
   out.internal.type = -1;
 
@@ -413,7 +437,8 @@ std::string build_box_mesh(const MeshSpec& spec, HostMesh& out) {
   for (int side = 0; side < 6; ++side) {
     int32_t t = spec.bc_override[side] >= 0 ? spec.bc_override[side] : default_types[side];
     if (t < 0 || t > 3) return "invalid boundary condition type";
-    fill_face_set(out.bc[side], raw, side_ids[side], xyz);
+    const std::string err = fill_face_set(out.bc[side], raw, side_ids[side], xyz, engine);
+    if (!err.empty()) return "device geometry: " + err;
     out.bc[side].type = t;
     out.bc[side].name = names[t];
   }

@@ -58,8 +58,32 @@ struct MeshSpec {
   int32_t bc_override[6] = {-1, -1, -1, -1, -1, -1};
 };
 
+// Where the per-item geometry is computed: face centroids, area vectors and
+// Roe frames (kokkos/Face.C:37-98) and cell volumes and centroids
+// (kokkos/MeshProcessor.C:130-171, ElementTopoHexa8.C:62-148). The default is
+// the host's threads; an engine may compute the same values elsewhere (the
+// device, miniaero_gb300/csrc/device/geometry.cu) with the same operation
+// order and rounding, so every result is bit-identical. Face and cell order,
+// the shuffle and the BinSort stay on the host.
+class GeometryEngine {
+ public:
+  virtual ~GeometryEngine() = default;
+  // Node coordinates [nnodes*3] for the calls that follow.
+  virtual std::string set_nodes(const double* xyz, size_t nnodes) = 0;
+  // For n faces given by their 4 nodes in creation order ([n*4]): centroid,
+  // area vector, tangent and binormal, each [n*3].
+  virtual std::string faces(size_t n, const int32_t* nodes4, double* coords, double* normal, double* tangent,
+                            double* binormal) = 0;
+  // For ncells Hexa8 cells ([ncells*8] nodes): volume [ncells] and centroid
+  // [ncells*3]; *negative += Gauss points whose Jacobian determinant is below
+  // 1e-300.
+  virtual std::string cells(size_t ncells, const int32_t* conn8, double* volume, double* centroid,
+                            int* negative) = 0;
+};
+
 // Builds the mesh. Returns an empty string on success, else a message.
-std::string build_box_mesh(const MeshSpec& spec, HostMesh& out);
+// engine: where the geometry is computed (nullptr: the host's threads).
+std::string build_box_mesh(const MeshSpec& spec, HostMesh& out, GeometryEngine* engine = nullptr);
 
 // glibc random()/rand() (TYPE_3 additive feedback generator, default seed 1).
 class GlibcRand {

@@ -180,7 +180,7 @@ ma_status ensure_mesh(ma_server* s, Request& q, CachedMesh** out) {
     cm.bytes = dry_mesh_bytes(s, q.req);
   } else {
     ma_options o = options_of(s, q.req);
-    ma_status st = ma_host_mesh_build(&o, &cm.host);
+    ma_status st = ma_host_mesh_build_ex(&o, MA_HOST_MESH_DEVICE_GEOMETRY, &cm.host);
     if (st != MA_OK) return st;
     ma_mesh_view v;
     ma_host_mesh_view(cm.host, &v);
@@ -246,7 +246,7 @@ void mesher_loop(ma_server* s) {
     std::string msg;
     {
       miniaero::TraceRange trace("ma_server_mesh_build");
-      st = ma_host_mesh_build(&o, &cm.host);
+      st = ma_host_mesh_build_ex(&o, MA_HOST_MESH_DEVICE_GEOMETRY, &cm.host);
       if (st == MA_OK) {
         ma_mesh_view v;
         ma_host_mesh_view(cm.host, &v);

@@ -406,6 +406,15 @@ ma_status ma_debug_check_division(int32_t mode, uint64_t n, uint64_t seed, uint6
  * are measured against. */
 ma_status ma_debug_fp64_rate(int32_t op, double* inst_per_s);
 
+/* Failure path of the grid barrier that separates the phases of the batch's
+ * single-launch step (ma_batch_set_single_launch): a cooperative launch of 2
+ * blocks in which block 1 returns at once, so block 0's wait at the barrier
+ * runs out after timeout_s (at most 10 s) instead of completing. Returns
+ * whether block 0 passed the barrier (*passed, 0 expected), the error word
+ * it left (*error_word, 1 expected) and the host-measured duration. The
+ * device context stays usable. */
+ma_status ma_debug_barrier_timeout(double timeout_s, int32_t* passed, int32_t* error_word, double* waited_s);
+
 /* ---- operator-level entry points (unit parity; host arrays in and out) --- */
 /* roe_flux::compute_flux (Roe_Flux.h:50) on n independent faces:
  * pl, pr [n*5] primitives; normal, tangent, binormal [n*3]; flux [n*5]. */

@@ -205,6 +205,7 @@ _SIGNATURES = {
     "ma_batch_get_launch": (c_int32, [c_void_p, P_i32, P_i32]),
     "ma_batch_set_launch": (c_int32, [c_void_p, P_i32, P_i32]),
     "ma_batch_set_single_launch": (c_int32, [c_void_p, c_int32, P_i32]),
+    "ma_debug_barrier_timeout": (c_int32, [c_double, P_i32, P_i32, ctypes.POINTER(c_double)]),
     "ma_batch_autotune": (c_int32, [c_void_p, c_int32, P_f64]),
     "ma_batch_profile_steps": (c_int32, [c_void_p, c_int32, P_f64, P_i32]),
     "ma_server_create": (c_int32, [ctypes.POINTER(ma_options), ctypes.c_size_t, c_int32, c_int32, c_int32,

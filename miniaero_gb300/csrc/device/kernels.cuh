@@ -170,6 +170,10 @@ cudaError_t launch_batch_steps_mixed(const PathConfig& cfg, const void* segs, co
 cudaError_t launch_batch_steps_fp64_fma(const PathConfig& cfg, const void* segs, const BatchLaunch& bl, int nsteps,
                                         unsigned* barrier_words, int* err, int block, int grid, cudaStream_t stream);
 cudaError_t batch_steps_occupancy_fp64(const PathConfig& cfg, int block, int* blocks_per_sm);
+// The grid barrier's failure path: a 2-block cooperative launch in which one
+// block never reaches the barrier; out[0] = passed (0), out[1] = error word (1).
+cudaError_t launch_debug_barrier_timeout(unsigned* words, int* err, unsigned long long timeout_ns, int* out,
+                                        cudaStream_t stream);
 cudaError_t batch_steps_occupancy_mixed(const PathConfig& cfg, int block, int* blocks_per_sm);
 cudaError_t batch_steps_occupancy_fp64_fma(const PathConfig& cfg, int block, int* blocks_per_sm);
 

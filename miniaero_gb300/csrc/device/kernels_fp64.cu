@@ -34,5 +34,11 @@ cudaError_t batch_steps_occupancy_fp64(const PathConfig& cfg, int block, int* bl
   return batch_steps_occupancy_impl<double>(cfg, block, blocks_per_sm);
 }
 
+cudaError_t launch_debug_barrier_timeout(unsigned* words, int* err, unsigned long long timeout_ns, int* out,
+                                        cudaStream_t stream) {
+  void* args[] = {(void*)&words, (void*)&err, (void*)&timeout_ns, (void*)&out};
+  return cudaLaunchCooperativeKernel((const void*)k_debug_barrier_timeout, dim3(2), dim3(32), args, 0, stream);
+}
+
 }  // namespace dev
 }  // namespace miniaero

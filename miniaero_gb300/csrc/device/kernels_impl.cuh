@@ -921,7 +921,8 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // Sense by generation: the last block to arrive resets the count and bumps
 // the generation; the others wait for the bump. Returns false when the
 // barrier gave up (timeout here or in another block).
-__device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned* gen, int* err) {
+__device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned* gen, int* err,
+                                             unsigned long long timeout_ns = kGridBarrierTimeoutNs) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -936,10 +937,13 @@ __device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned* gen, int
       atomicAdd(gen, 1u);
     } else {
       const unsigned long long t0 = global_ns();
+      unsigned spins = 0;
       while (ok && *vgen == g) {
         __nanosleep(64);
         if (*verr != 0) ok = 0;
-        else if (global_ns() - t0 > kGridBarrierTimeoutNs) {
+        // The time limit, and an iteration limit that holds even if the
+        // timer did not advance (2^28 sleeps of at least 64 ns: over 17 s).
+        else if (global_ns() - t0 > timeout_ns || ++spins > (1u << 28)) {
           atomicExch(err, 1);
           ok = 0;
         }
@@ -1052,6 +1056,19 @@ cudaError_t batch_steps_occupancy_impl(const PathConfig& cfg, int block, int* bl
   }
   const size_t smem = (mode == 1 && std::is_same<R, double>::value) ? block / 32 * kVenkatBufBytes : 0;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, block, smem);
+}
+
+// Failure path of the grid barrier: block 0 waits at a barrier that block 1
+// never reaches (it returns at once), so the wait runs out after timeout_ns;
+// out[0] = whether block 0 passed the barrier (0 expected), out[1] = the
+// error word afterwards (1 expected).
+__global__ void k_debug_barrier_timeout(unsigned* words, int* err, unsigned long long timeout_ns, int* out) {
+  if (blockIdx.x != 0) return;
+  const bool passed = grid_barrier(words, words + 1, err, timeout_ns);
+  if (threadIdx.x == 0) {
+    out[0] = passed ? 1 : 0;
+    out[1] = *static_cast<volatile int*>(err);
+  }
 }
 
 // Primitives of U_n + 0 * res with res = 0 (first stage after set_state).

@@ -13,6 +13,7 @@
 //    sets in boundary_faces order (GreenGauss.h:300-321, StencilLimiter.h:532-616)
 //    or grouped by BC type (TimeSolverExplicitRK4.h:428-475) for the residual.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -908,6 +909,12 @@ struct DevBufs {
     ptrs.push_back(*d);
     return h ? cudaMemcpy(*d, h, sizeof(double) * n, cudaMemcpyHostToDevice) : cudaSuccess;
   }
+  template <class T>
+  cudaError_t in(std::nullptr_t, size_t n, T** d) {
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(d), sizeof(T) * (n ? n : 1));
+    if (e == cudaSuccess) ptrs.push_back(*d);
+    return e;
+  }
 };
 
 }  // namespace
@@ -1006,6 +1013,31 @@ extern "C" ma_status ma_debug_fp64_rate(int32_t op, double* inst_per_s) {
   MA_CUDA_TRY(err);
   if (!(best > 0.f)) return set_error(MA_ENUMERIC, "ma_debug_fp64_rate: no elapsed time");
   *inst_per_s = static_cast<double>(blocks) * 256.0 * iters * 4.0 / (best * 1e-3);
+  return MA_OK;
+}
+
+extern "C" ma_status ma_debug_barrier_timeout(double timeout_s, int32_t* passed, int32_t* error_word,
+                                              double* waited_s) {
+  if (!passed || !error_word || !waited_s || !(timeout_s > 0.0) || timeout_s > 10.0)
+    return set_error(MA_EINVAL, "ma_debug_barrier_timeout: bad arguments (timeout in (0, 10] s)");
+  DevBufs b;
+  unsigned* words;
+  int* err;
+  int* out;
+  MA_CUDA_TRY(b.in(nullptr, 2, &words));
+  MA_CUDA_TRY(b.in(nullptr, 1, &err));
+  MA_CUDA_TRY(b.in(nullptr, 2, &out));
+  MA_CUDA_TRY(cudaMemset(words, 0, 2 * sizeof(unsigned)));
+  MA_CUDA_TRY(cudaMemset(err, 0, sizeof(int)));
+  MA_CUDA_TRY(cudaMemset(out, 0xFF, 2 * sizeof(int)));
+  const auto t0 = std::chrono::steady_clock::now();
+  MA_CUDA_TRY(dev::launch_debug_barrier_timeout(words, err, static_cast<unsigned long long>(timeout_s * 1e9), out, 0));
+  MA_CUDA_TRY(cudaDeviceSynchronize());
+  *waited_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  int host[2];
+  MA_CUDA_TRY(cudaMemcpy(host, out, sizeof(host), cudaMemcpyDeviceToHost));
+  *passed = host[0];
+  *error_word = host[1];
   return MA_OK;
 }
 

@@ -189,3 +189,27 @@ def test_single_launch_steps_equal_single_solves(has_gpu, precision, second, vis
     b.close()
     for dm in meshes + [dx]:
         dm.close()
+
+
+def test_grid_barrier_wait_runs_out_and_reports(has_gpu):
+    """The single-launch step's grid barrier bounds every wait: a launch in
+    which one block never reaches the barrier makes the other give up after
+    the limit, leave the error word set and return; the device stays usable
+    (a batch steps afterwards with the bits of its solves alone)."""
+    import ctypes
+    from miniaero_gb300._lib import check, lib
+    passed, err, waited = ctypes.c_int32(-1), ctypes.c_int32(-1), ctypes.c_double(0.0)
+    check(lib().ma_debug_barrier_timeout(0.05, ctypes.byref(passed), ctypes.byref(err), ctypes.byref(waited)))
+    assert passed.value == 0 and err.value == 1
+    assert 0.05 <= waited.value < 5.0
+    o = sod_options(ma.MA_PREC_FP64)
+    m, md, U0 = member(o, (10, 6, 4), 4.0, 3.0)
+    dm = ma.DeviceMesh(md)
+    b = ma.Batch(o, capacity=2)
+    b.set_single_launch(128)
+    i = b.add(dm, U0)
+    b.step(3)
+    b.synchronize()
+    assert np.array_equal(b.get_state(i), single(md, m, U0, 3, b.member_dt(i)))
+    b.close()
+    dm.close()

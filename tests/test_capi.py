@@ -66,6 +66,15 @@ def test_extension_keys(tmp_path):
     assert o.bc_override[0] == ma.MA_BC_NOSLIP and o.keep_residual == 1
 
 
+def test_precision_keys(tmp_path):
+    base = "0\n1 1 1 0\n4 4 4\n10\n1e-5\n0\n1\n0\n0\n"
+    for word, want in (("fp64", ma.MA_PREC_FP64), ("mixed", ma.MA_PREC_MIXED), ("fp64_fma", ma.MA_PREC_FP64_FMA)):
+        o = ma.Options.read_options_file(write(tmp_path, base + "precision %s\n" % word))
+        assert o.precision == want
+    with pytest.raises(ma.MiniaeroError):
+        ma.Options.read_options_file(write(tmp_path, base + "precision fp16\n"))
+
+
 @pytest.mark.parametrize("text", ["0\n1 1 1 0\n4 4\n", "0\n1 1 1 0\n4 4 4\n10\n1e-5\n0\n1\n0\n0\nbogus 3\n",
                                   "0\n1 1 1 0\n4 4 4\n10\n1e-5\n0\n1\n0\n0\nlimiter minmod\n"])
 def test_malformed_inputs_are_errors(tmp_path, text):

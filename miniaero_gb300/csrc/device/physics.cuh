@@ -360,6 +360,47 @@ __device__ __forceinline__ void roe_flux_axis(const R pl[5], const R pr[5], R nD
   const R ep3 = R(0.5) * (eig3 + a3), em3 = R(0.5) * (eig3 - a3);
   const R lam[5] = {ep1 - em1, ep2 - em2, ep3 - em3, ep3 - em3, ep3 - em3};
 
+  if constexpr (std::is_same<R, float>::value) {
+    // Mixed form: the same dissipation |A| dU evaluated by wave strengths
+    // instead of the two eigenvector products (the mixed form keeps no
+    // reference bits). The strengths come from the conserved jumps dq with
+    // the reference's gm1 = 0.4, exactly as its left eigenvectors take them
+    // (its gas has cp 1004 and R 287.05, so a pressure jump from p = rho R T
+    // would not be the same quantity): with P = gm1 (dq4 - v~.dqm + ke dq0)
+    // and mn = n.dqm - u~n dq0, the rows give L0.dq = P + c mn, L1.dq =
+    // P - c mn, L2.dq = P/gm1 - hroe dq0, L3.dq = tu (dqm_T - v~_T dq0),
+    // L4.dq = bu (dqm_B - v~_B dq0); the right eigenvectors turn them into
+    // the acoustic, entropy and shear waves below (c^2 = gm1 hroe). lam
+    // already carries the face area and the entropy fix (lam[0] the u+c
+    // wave, lam[1] u-c, lam[2] u).
+    const R dq0 = rr - rl;
+    R dqm[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) dqm[j] = rr * vel_r[j] - rl * vel_l[j];
+    const R dq4 = (rr * H_r - p_r) - (rl * H_l - p_l);
+    const R P = gm1 * (dq4 - (vroe[0] * dqm[0] + vroe[1] * dqm[1] + vroe[2] * dqm[2]) + ke * dq0);
+    const R mn = (dqm[D] - vroe[D] * dq0) * nuD;
+    const R h2 = R(0.5) * cssi;
+    const R cmn = c * mn;
+    const R w5 = lam[0] * ((P + cmn) * h2);   // u + c wave
+    const R w1 = lam[1] * ((P - cmn) * h2);   // u - c wave
+    const R w2 = lam[2] * (dq0 - P * cssi);   // entropy wave
+    const R sT = lam[2] * (dqm[T] - vroe[T] * dq0);  // shear waves
+    const R sB = lam[2] * (dqm[B] - vroe[B] * dq0);
+    const R wsum = w1 + w2 + w5;
+    const R cun = c * (vroe[D] * nuD);
+    const R hk = hroe + ke;
+    R dis[5];
+    dis[0] = wsum;
+    dis[1 + D] = wsum * vroe[D] + (c * nuD) * (w5 - w1);
+    dis[1 + T] = wsum * vroe[T] + sT;
+    dis[1 + B] = wsum * vroe[B] + sB;
+    dis[4] = w1 * (hk - cun) + w5 * (hk + cun) + w2 * ke + (vroe[T] * sT + vroe[B] * sB);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) flux[k] -= R(0.5) * dis[k];
+    return;
+  }
+
   // Left eigenvectors: rows 0/1 hold c*nu_j - gm1*u_j (c*nu_j = +-0 off D),
   // rows 3/4 have a single nonzero tangent/binormal entry.
   const R gk = gm1 * (ke - hroe);

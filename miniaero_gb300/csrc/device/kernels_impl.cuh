@@ -600,10 +600,16 @@ __device__ __forceinline__ void internal_flux_face(const TopoView& t, const Geom
       const R dl = g.dL[D * F + f], dr = g.dR[D * F + f];
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
-        const R tl = R(0) + dl * grad[(3 * k + D) * C + L];
-        const R trr = R(0) + dr * grad[(3 * k + D) * C + Rc];
-        pl[k] += tl * phi[k * C + L];
-        pr[k] += trr * phi[k * C + Rc];
+        if constexpr (std::is_same<R, float>::value) {
+          // Mixed form: one fused multiply-add per side (no reference bits to keep).
+          pl[k] = fmaf(dl * grad[(3 * k + D) * C + L], phi[k * C + L], pl[k]);
+          pr[k] = fmaf(dr * grad[(3 * k + D) * C + Rc], phi[k * C + Rc], pr[k]);
+        } else {
+          const R tl = R(0) + dl * grad[(3 * k + D) * C + L];
+          const R trr = R(0) + dr * grad[(3 * k + D) * C + Rc];
+          pl[k] += tl * phi[k * C + L];
+          pr[k] += trr * phi[k * C + Rc];
+        }
       }
     } else {
       const R dl[3] = {g.dL[f], g.dL[F + f], g.dL[2 * F + f]};

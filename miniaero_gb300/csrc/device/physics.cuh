@@ -294,9 +294,103 @@ __device__ __forceinline__ void roe_flux(const R pl[5], const R pr[5], const Fac
 // the reference's order, so every nonzero intermediate equals roe_flux's. A
 // zero intermediate may differ in sign only; none reaches a division, a
 // square root or a comparison that could tell.
+// The mixed form's Roe flux on an axis-aligned face (FP32; the mixed form
+// keeps no reference bits). Same central flux, Roe averages and entropy fix
+// as roe_flux_axis, with a*b+c written as fused multiply-adds (explicit
+// fmaf: the same bits in every kernel that inlines it, so batch and single
+// runs agree), and the dissipation |A| dU evaluated as its acoustic, entropy
+// and shear waves instead of the two eigenvector products. The wave
+// strengths come from the conserved jumps dq with the reference's gm1 = 0.4,
+// as its left eigenvectors take them (its gas has cp 1004 and R 287.05, so a
+// strength built on the jump of p = rho R T would be a different scheme):
+// with P = gm1 (dq4 - v~.dqm + ke dq0) and mn = n.dqm - u~n dq0 the rows give
+// L0.dq = P + c mn, L1.dq = P - c mn, L2.dq = P/gm1 - hroe dq0, L3.dq =
+// tu (dqm_T - v~_T dq0) and L4.dq = bu (dqm_B - v~_B dq0), and the right
+// eigenvectors (with c^2 = gm1 hroe) turn them into the waves below.
+template <int D>
+__device__ __forceinline__ void roe_flux_axis_f32(const float pl[5], const float pr[5], float nD, float nuD,
+                                                  float nn, float flux[5]) {
+  constexpr int T = (D + 2) % 3, B = (D + 1) % 3;
+  const float gm1 = 0.4f, efix = 0.1f;
+  const float rl = pl[0], rr = pr[0];
+  const float vl[3] = {pl[1], pl[2], pl[3]};
+  const float vr[3] = {pr[1], pr[2], pr[3]};
+  const float p_l = rl * 287.05f * pl[4], p_r = rr * 287.05f * pr[4];
+  const float h_l = 1004.0f * pl[4], h_r = 1004.0f * pr[4];
+  const float H_l = fmaf(0.5f, fmaf(vl[0], vl[0], fmaf(vl[1], vl[1], vl[2] * vl[2])), h_l);
+  const float H_r = fmaf(0.5f, fmaf(vr[0], vr[0], fmaf(vr[1], vr[1], vr[2] * vr[2])), h_r);
+  const float mf_l = rl * (nD * vl[D]), mf_r = rr * (nD * vr[D]);
+
+  flux[0] = 0.5f * (mf_l + mf_r);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    float m = fmaf(mf_l, vl[j], mf_r * vr[j]);
+    if (j == D) m = fmaf(nD, p_l + p_r, m);
+    flux[1 + j] = 0.5f * m;
+  }
+  flux[4] = 0.5f * fmaf(mf_l, H_l, mf_r * H_r);
+
+  const float srl = sqrtf(rl), srr = sqrtf(rr);
+  const float alpha = srl / (srl + srr);
+  const float beta = 1.0f - alpha;
+  float vroe[3], dv[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    vroe[j] = fmaf(alpha, vl[j], beta * vr[j]);
+    dv[j] = vr[j] - vl[j];
+  }
+  const float dv2 = fmaf(dv[0], dv[0], fmaf(dv[1], dv[1], dv[2] * dv[2]));
+  const float hroe = fmaf(alpha, h_l, fmaf(beta, h_r, 0.5f * alpha * beta * dv2));
+  const float c = sqrtf(gm1 * hroe);
+  const float ke = 0.5f * fmaf(vroe[0], vroe[0], fmaf(vroe[1], vroe[1], vroe[2] * vroe[2]));
+  const float cssi = 1.0f / (c * c);
+
+  // Eigenvalues (with the face area) and the entropy fix of the reference.
+  const float cbar = c * nn;
+  const float ubar = vroe[D] * nD;
+  const float cfl = fabsf(ubar) + cbar;
+  const float eig1 = ubar + cbar, eig2 = ubar - cbar, eig3 = ubar;
+  float a1 = fabsf(eig1), a2 = fabsf(eig2), a3 = fabsf(eig3);
+  const float ep = efix * cfl;
+  if (a1 < ep) a1 = 0.5f * fmaf(eig1, eig1, ep * ep) / ep;
+  if (a2 < ep) a2 = 0.5f * fmaf(eig2, eig2, ep * ep) / ep;
+  if (a3 < ep) a3 = 0.5f * fmaf(eig3, eig3, ep * ep) / ep;
+
+  // Conserved jumps and wave strengths (a1: the u+c wave, a2: u-c, a3: u).
+  const float dq0 = rr - rl;
+  float dqm[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) dqm[j] = fmaf(rr, vr[j], -(rl * vl[j]));
+  const float dq4 = fmaf(rr, H_r, -p_r) - fmaf(rl, H_l, -p_l);
+  const float vdq = fmaf(vroe[0], dqm[0], fmaf(vroe[1], dqm[1], vroe[2] * dqm[2]));
+  const float P = gm1 * fmaf(ke, dq0, dq4 - vdq);
+  const float cmn = c * (fmaf(-vroe[D], dq0, dqm[D]) * nuD);
+  const float h2 = 0.5f * cssi;
+  const float w5 = a1 * ((P + cmn) * h2);
+  const float w1 = a2 * ((P - cmn) * h2);
+  const float w2 = a3 * fmaf(-P, cssi, dq0);
+  const float sT = a3 * fmaf(-vroe[T], dq0, dqm[T]);
+  const float sB = a3 * fmaf(-vroe[B], dq0, dqm[B]);
+  const float wsum = w1 + w2 + w5;
+  const float cun = c * (vroe[D] * nuD);
+  const float hk = hroe + ke;
+  float dis[5];
+  dis[0] = wsum;
+  dis[1 + D] = fmaf(wsum, vroe[D], (c * nuD) * (w5 - w1));
+  dis[1 + T] = fmaf(wsum, vroe[T], sT);
+  dis[1 + B] = fmaf(wsum, vroe[B], sB);
+  dis[4] = fmaf(w1, hk - cun, fmaf(w5, hk + cun, fmaf(w2, ke, fmaf(vroe[T], sT, vroe[B] * sB))));
+#pragma unroll
+  for (int k = 0; k < 5; ++k) flux[k] = fmaf(-0.5f, dis[k], flux[k]);
+}
+
 template <class R, int D>
 __device__ __forceinline__ void roe_flux_axis(const R pl[5], const R pr[5], R nD, R nuD, R tuT, R buB, R nn,
                                               R flux[5]) {
+  if constexpr (std::is_same<R, float>::value) {
+    roe_flux_axis_f32<D>(pl, pr, nD, nuD, nn, flux);
+    return;
+  }
   constexpr int T = (D + 2) % 3, B = (D + 1) % 3;
   const R efix_u = R(0.1), efix_c = R(0.1), gm1 = R(0.4);
   const R rl = pl[0];
@@ -360,46 +454,6 @@ __device__ __forceinline__ void roe_flux_axis(const R pl[5], const R pr[5], R nD
   const R ep3 = R(0.5) * (eig3 + a3), em3 = R(0.5) * (eig3 - a3);
   const R lam[5] = {ep1 - em1, ep2 - em2, ep3 - em3, ep3 - em3, ep3 - em3};
 
-  if constexpr (std::is_same<R, float>::value) {
-    // Mixed form: the same dissipation |A| dU evaluated by wave strengths
-    // instead of the two eigenvector products (the mixed form keeps no
-    // reference bits). The strengths come from the conserved jumps dq with
-    // the reference's gm1 = 0.4, exactly as its left eigenvectors take them
-    // (its gas has cp 1004 and R 287.05, so a pressure jump from p = rho R T
-    // would not be the same quantity): with P = gm1 (dq4 - v~.dqm + ke dq0)
-    // and mn = n.dqm - u~n dq0, the rows give L0.dq = P + c mn, L1.dq =
-    // P - c mn, L2.dq = P/gm1 - hroe dq0, L3.dq = tu (dqm_T - v~_T dq0),
-    // L4.dq = bu (dqm_B - v~_B dq0); the right eigenvectors turn them into
-    // the acoustic, entropy and shear waves below (c^2 = gm1 hroe). lam
-    // already carries the face area and the entropy fix (lam[0] the u+c
-    // wave, lam[1] u-c, lam[2] u).
-    const R dq0 = rr - rl;
-    R dqm[3];
-#pragma unroll
-    for (int j = 0; j < 3; ++j) dqm[j] = rr * vel_r[j] - rl * vel_l[j];
-    const R dq4 = (rr * H_r - p_r) - (rl * H_l - p_l);
-    const R P = gm1 * (dq4 - (vroe[0] * dqm[0] + vroe[1] * dqm[1] + vroe[2] * dqm[2]) + ke * dq0);
-    const R mn = (dqm[D] - vroe[D] * dq0) * nuD;
-    const R h2 = R(0.5) * cssi;
-    const R cmn = c * mn;
-    const R w5 = lam[0] * ((P + cmn) * h2);   // u + c wave
-    const R w1 = lam[1] * ((P - cmn) * h2);   // u - c wave
-    const R w2 = lam[2] * (dq0 - P * cssi);   // entropy wave
-    const R sT = lam[2] * (dqm[T] - vroe[T] * dq0);  // shear waves
-    const R sB = lam[2] * (dqm[B] - vroe[B] * dq0);
-    const R wsum = w1 + w2 + w5;
-    const R cun = c * (vroe[D] * nuD);
-    const R hk = hroe + ke;
-    R dis[5];
-    dis[0] = wsum;
-    dis[1 + D] = wsum * vroe[D] + (c * nuD) * (w5 - w1);
-    dis[1 + T] = wsum * vroe[T] + sT;
-    dis[1 + B] = wsum * vroe[B] + sB;
-    dis[4] = w1 * (hk - cun) + w5 * (hk + cun) + w2 * ke + (vroe[T] * sT + vroe[B] * sB);
-#pragma unroll
-    for (int k = 0; k < 5; ++k) flux[k] -= R(0.5) * dis[k];
-    return;
-  }
 
   // Left eigenvectors: rows 0/1 hold c*nu_j - gm1*u_j (c*nu_j = +-0 off D),
   // rows 3/4 have a single nonzero tangent/binormal entry.

@@ -923,8 +923,13 @@ def run_serving_suite(ma, n_requests=32, rate=200.0, loads=(0.25, 0.5, 0.9), n_l
     for dev in (False, True):
         ma.Parallel3DMesh.from_options(mo).fill_mesh_data(device_geometry=dev)  # warm (module load)
         t0 = time.perf_counter()
-        ma.Parallel3DMesh.from_options(mo).fill_mesh_data(device_geometry=dev)
+        md128 = ma.Parallel3DMesh.from_options(mo).fill_mesh_data(device_geometry=dev)
         times["device_geometry" if dev else "host_geometry"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    dm128 = ma.DeviceMesh(md128)
+    times["device_upload"] = time.perf_counter() - t0
+    dm128.close()
+    del md128
     out["mesh_build_128_cubed_s"] = times
     # The 50 % load again with an empty mesh cache: every first request of a
     # size waits for its mesh, built by the server's mesh thread while the

@@ -430,7 +430,7 @@ __device__ __forceinline__ void green_gauss_cell(const TopoView& t, const GeomVi
         for (int k = 0; k < 5; ++k) {
           const R pl = left ? wc[k] : wn[k];
           const R pr = left ? wn[k] : wc[k];
-          const R gr = R(0.5) * (pl + pr) * np;
+          const R gr = halve(pl + pr) * np;
           acc[k][p] += div(left ? gr : -gr);
           if (MINMAX) ex[k].face(pl, pr);
         }
@@ -480,7 +480,7 @@ __device__ __noinline__ void gradient_exact(const TopoView& t, const GeomView<do
   green_gauss_cell<double, false>(t, g, W, c, wc, acc, static_cast<Extrema<double>*>(nullptr),
                                   [&](double a) { return a / V; });
   for (int k = 0; k < 5; ++k)
-    for (int d = 0; d < 3; ++d) grad[(3 * k + d) * C + c] = 0.0 + acc[k][d];
+    for (int d = 0; d < 3; ++d) grad[(3 * k + d) * C + c] = zero_plus(acc[k][d]);
 }
 
 // MODE: 0 gradient only (viscous first order), 1 + Venkatakrishnan, 2 + Van Albada.
@@ -530,7 +530,7 @@ __device__ __forceinline__ void sweep1_cell(const TopoView& t, const GeomView<R>
     for (int k = 0; k < 5; ++k)
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
-        gsum[k][d] = R(0) + acc[k][d];  // green_gauss_gradient_sum
+        gsum[k][d] = zero_plus(acc[k][d]);  // green_gauss_gradient_sum: 0 + sum
         if (valid) grad[(3 * k + d) * C + c] = gsum[k][d];
       }
   }
@@ -566,9 +566,9 @@ __device__ __forceinline__ void face_flux_axis(const TopoView& t, const GeomView
     R pf[5], gf[5][3], vf[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
-      pf[k] = R(0.5) * (pl[k] + pr[k]);
+      pf[k] = halve(pl[k] + pr[k]);
 #pragma unroll
-      for (int d = 0; d < 3; ++d) gf[k][d] = R(0.5) * (grad[(3 * k + d) * C + L] + grad[(3 * k + d) * C + Rc]);
+      for (int d = 0; d < 3; ++d) gf[k][d] = halve(grad[(3 * k + d) * C + L] + grad[(3 * k + d) * C + Rc]);
     }
     viscous_flux_axis<R, D>(gf, pf, nD, tr, vf);
 #pragma unroll
@@ -605,8 +605,8 @@ __device__ __forceinline__ void internal_flux_face(const TopoView& t, const Geom
           pl[k] = fmaf(dl * grad[(3 * k + D) * C + L], phi[k * C + L], pl[k]);
           pr[k] = fmaf(dr * grad[(3 * k + D) * C + Rc], phi[k * C + Rc], pr[k]);
         } else {
-          const R tl = R(0) + dl * grad[(3 * k + D) * C + L];
-          const R trr = R(0) + dr * grad[(3 * k + D) * C + Rc];
+          const R tl = zero_plus(dl * grad[(3 * k + D) * C + L]);
+          const R trr = zero_plus(dr * grad[(3 * k + D) * C + Rc]);
           pl[k] += tl * phi[k * C + L];
           pr[k] += trr * phi[k * C + Rc];
         }
@@ -766,7 +766,9 @@ __device__ __forceinline__ void residual_cell(const TopoView& t, const R* __rest
       if (cell_flux) {
         acc[k] = acc[k] + dtv * v;
       } else {
-        acc[k] += v;  // the plain form adds to +0 as the reference does
+        // the plain form adds to +0 as the reference does; with the first
+        // slot present its term is 0 + v
+        acc[k] = s == 0 ? zero_plus(v) : acc[k] + v;
       }
     }
   }
@@ -791,7 +793,7 @@ __device__ __forceinline__ void residual_cell(const TopoView& t, const R* __rest
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
     // 0.0 + x as in apply_cell_flux (it only normalises a -0 result).
-    const double r = cell_flux ? acc[k] : kPlain ? 0.0 + dtv * acc[k] : acc[k];
+    const double r = cell_flux ? acc[k] : kPlain ? zero_plus(dtv * acc[k]) : acc[k];
     if (res_out) res_out[k * C + c] = fold ? dtv * acc[k] : r;
     // x + a*r: the plain form rounds the product and the sum as the
     // reference does; the mixed form (FP64 update, no reference bits to keep)

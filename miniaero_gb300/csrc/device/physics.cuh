@@ -55,6 +55,29 @@ __device__ __forceinline__ double div_by_recip(double a, double b, double y) {
 }
 __device__ __forceinline__ float div_by_recip(float a, float /*b*/, float y) { return a * y; }
 
+// Exact FP64 identities taken off the FP64 pipe, which bounds the plain form
+// on GB300 (2 FP64 lanes per SM per clock): the integer ALU gives the same
+// bits in a few instructions.
+//
+// halve(x) = 0.5 * x: for a normal x above the smallest binade the exponent
+// field steps down by one (the product is exact); zeros, subnormals, the
+// smallest binade, infinities and NaNs take the multiply.
+__device__ __forceinline__ double halve(double x) {
+  const uint32_t hi = static_cast<uint32_t>(__double2hiint(x));
+  if (((hi >> 20) & 0x7FFu) - 2u < 2045u)
+    return __hiloint2double(static_cast<int>(hi - 0x100000u), __double2loint(x));
+  return 0.5 * x;
+}
+__device__ __forceinline__ float halve(float x) { return 0.5f * x; }
+// zero_plus(x) = 0 + x in round to nearest: x itself, except that -0 becomes
+// +0 (a sum that starts at +0 and adds x). A NaN stays a NaN.
+__device__ __forceinline__ double zero_plus(double x) {
+  const uint32_t hi = static_cast<uint32_t>(__double2hiint(x));
+  const bool negzero = (hi == 0x80000000u) & (__double2loint(x) == 0);
+  return __hiloint2double(negzero ? 0 : static_cast<int>(hi), __double2loint(x));
+}
+__device__ __forceinline__ float zero_plus(float x) { return 0.0f + x; }
+
 // The reciprocal-method quotient without the IEEE fallback, for hot loops
 // that handle the rare cases out of line: `inexact` is set when the quotient
 // may differ from a/b (the conditions of div_by_recip, with zero numerators
@@ -397,22 +420,22 @@ __device__ __forceinline__ void roe_flux_axis(const R pl[5], const R pr[5], R nD
   const R vel_l[3] = {pl[1], pl[2], pl[3]};
   const R p_l = rl * R(287.05) * pl[4];
   const R h_l = R(1004.0) * pl[4];
-  const R H_l = h_l + R(0.5) * (vel_l[0] * vel_l[0] + vel_l[1] * vel_l[1] + vel_l[2] * vel_l[2]);
+  const R H_l = h_l + halve(vel_l[0] * vel_l[0] + vel_l[1] * vel_l[1] + vel_l[2] * vel_l[2]);
   const R mf_l = rl * (nD * vel_l[D]);
   const R rr = pr[0];
   const R vel_r[3] = {pr[1], pr[2], pr[3]};
   const R p_r = rr * R(287.05) * pr[4];
   const R h_r = R(1004.0) * pr[4];
-  const R H_r = h_r + R(0.5) * (vel_r[0] * vel_r[0] + vel_r[1] * vel_r[1] + vel_r[2] * vel_r[2]);
+  const R H_r = h_r + halve(vel_r[0] * vel_r[0] + vel_r[1] * vel_r[1] + vel_r[2] * vel_r[2]);
   const R mf_r = rr * (nD * vel_r[D]);
   const R psum = p_l + p_r;
 
-  flux[0] = R(0.5) * (mf_l + mf_r);
+  flux[0] = halve(mf_l + mf_r);
 #pragma unroll
   for (int j = 0; j < 3; ++j)
-    flux[1 + j] = (j == D) ? R(0.5) * (mf_l * vel_l[j] + mf_r * vel_r[j] + nD * psum)
-                           : R(0.5) * (mf_l * vel_l[j] + mf_r * vel_r[j]);
-  flux[4] = R(0.5) * (mf_l * H_l + mf_r * H_r);
+    flux[1 + j] = (j == D) ? halve(mf_l * vel_l[j] + mf_r * vel_r[j] + nD * psum)
+                           : halve(mf_l * vel_l[j] + mf_r * vel_r[j]);
+  flux[4] = halve(mf_l * H_l + mf_r * H_r);
 
   const R srl = dsqrt<R>(rl);
   const R denom = R(1.0) / (srl + dsqrt<R>(rr));
@@ -422,7 +445,7 @@ __device__ __forceinline__ void roe_flux_axis(const R pl[5], const R pr[5], R nD
 #pragma unroll
   for (int j = 0; j < 3; ++j) vroe[j] = alpha * vel_l[j] + beta * vel_r[j];
   const R hroe = alpha * h_l + beta * h_r +
-                 R(0.5) * alpha * beta *
+                 halve(alpha) * beta *
                      ((vel_r[0] - vel_l[0]) * (vel_r[0] - vel_l[0]) + (vel_r[1] - vel_l[1]) * (vel_r[1] - vel_l[1]) +
                       (vel_r[2] - vel_l[2]) * (vel_r[2] - vel_l[2]));
   const R c = dsqrt<R>(gm1 * hroe);
@@ -430,9 +453,9 @@ __device__ __forceinline__ void roe_flux_axis(const R pl[5], const R pr[5], R nD
   const R nv = vroe[D] * nuD;
   const R tv = vroe[T] * tuT;
   const R bv = vroe[B] * buB;
-  const R ke = R(0.5) * (vroe[0] * vroe[0] + vroe[1] * vroe[1] + vroe[2] * vroe[2]);
+  const R ke = halve(vroe[0] * vroe[0] + vroe[1] * vroe[1] + vroe[2] * vroe[2]);
   const R cssi = R(1.0) / (c * c);
-  const R hcssi = R(0.5) * cssi;
+  const R hcssi = halve(cssi);
 
   R dq[5];
   dq[0] = rr - rl;
@@ -449,9 +472,9 @@ __device__ __forceinline__ void roe_flux_axis(const R pl[5], const R pr[5], R nD
   if (a1 < epcc) a1 = R(0.5) * (eig1 * eig1 + epcc * epcc) / epcc;
   if (a2 < epcc) a2 = R(0.5) * (eig2 * eig2 + epcc * epcc) / epcc;
   if (a3 < epuc) a3 = R(0.5) * (eig3 * eig3 + epuc * epuc) / epuc;
-  const R ep1 = R(0.5) * (eig1 + a1), em1 = R(0.5) * (eig1 - a1);
-  const R ep2 = R(0.5) * (eig2 + a2), em2 = R(0.5) * (eig2 - a2);
-  const R ep3 = R(0.5) * (eig3 + a3), em3 = R(0.5) * (eig3 - a3);
+  const R ep1 = halve(eig1 + a1), em1 = halve(eig1 - a1);
+  const R ep2 = halve(eig2 + a2), em2 = halve(eig2 - a2);
+  const R ep3 = halve(eig3 + a3), em3 = halve(eig3 - a3);
   const R lam[5] = {ep1 - em1, ep2 - em2, ep3 - em3, ep3 - em3, ep3 - em3};
 
 
@@ -470,22 +493,21 @@ __device__ __forceinline__ void roe_flux_axis(const R pl[5], const R pr[5], R nD
   row1[4] = gm1;
   R ldq[5];
   {
-    R a0 = R(0.0), b0 = R(0.0), c0 = R(0.0);
+    // Sums that start at +0: the first term is zero_plus (0 + x).
+    R a0 = zero_plus(row0[0] * dq[0]), b0 = zero_plus(row1[0] * dq[0]);
 #pragma unroll
-    for (int j = 0; j < 5; ++j) {
+    for (int j = 1; j < 5; ++j) {
       a0 += row0[j] * dq[j];
       b0 += row1[j] * dq[j];
     }
-    c0 += (ke - hroe) * dq[0];
+    R c0 = zero_plus((ke - hroe) * dq[0]);
     c0 += -vroe[0] * dq[1];
     c0 += -vroe[1] * dq[2];
     c0 += -vroe[2] * dq[3];
     c0 += R(1.0) * dq[4];
-    R d0 = R(0.0);
-    d0 += -tv * dq[0];
+    R d0 = zero_plus(-tv * dq[0]);
     d0 += tuT * dq[1 + T];
-    R e0 = R(0.0);
-    e0 += -bv * dq[0];
+    R e0 = zero_plus(-bv * dq[0]);
     e0 += buB * dq[1 + B];
     ldq[0] = lam[0] * a0;
     ldq[1] = lam[1] * b0;
@@ -496,35 +518,33 @@ __device__ __forceinline__ void roe_flux_axis(const R pl[5], const R pr[5], R nD
   // Right eigenvectors.
   const R hk = hroe + ke;
   {
-    R acc = R(0.0);
-    acc += hcssi * ldq[0];
+    R acc = zero_plus(hcssi * ldq[0]);
     acc += hcssi * ldq[1];
     acc += -gm1 * cssi * ldq[2];
-    flux[0] -= R(0.5) * acc;
+    flux[0] -= halve(acc);
   }
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
-    R acc = R(0.0);
+    R acc;
     if (j == D) {
-      acc += (vroe[j] + nuD * c) * hcssi * ldq[0];
+      acc = zero_plus((vroe[j] + nuD * c) * hcssi * ldq[0]);
       acc += (vroe[j] - nuD * c) * hcssi * ldq[1];
     } else {
-      acc += vroe[j] * hcssi * ldq[0];
+      acc = zero_plus(vroe[j] * hcssi * ldq[0]);
       acc += vroe[j] * hcssi * ldq[1];
     }
     acc += -gm1 * vroe[j] * cssi * ldq[2];
     if (j == T) acc += tuT * ldq[3];
     if (j == B) acc += buB * ldq[4];
-    flux[1 + j] -= R(0.5) * acc;
+    flux[1 + j] -= halve(acc);
   }
   {
-    R acc = R(0.0);
-    acc += (hk + c * nv) * hcssi * ldq[0];
+    R acc = zero_plus((hk + c * nv) * hcssi * ldq[0]);
     acc += (hk - c * nv) * hcssi * ldq[1];
     acc += (c * c - gm1 * hk) * cssi * ldq[2];
     acc += tv * ldq[3];
     acc += bv * ldq[4];
-    flux[4] -= R(0.5) * acc;
+    flux[4] -= halve(acc);
   }
 }
 
@@ -604,12 +624,11 @@ __device__ __forceinline__ void viscous_flux_axis(const R g[5][3], const R prim[
   R v4 = R(0.0);
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    const R S = R(0.5) * (g[i + 1][D] + g[D + 1][i]);
+    const R S = halve(g[i + 1][D] + g[D + 1][i]);
     const R tiD = (i == D) ? S - div3 : S;
-    R vi = R(0.0);
-    vi += (R(2) * mu * tiD) * aD;
-    vflux[1 + i] = vi;
-    v4 += (R(2) * mu * tiD) * prim[i + 1] * aD;
+    vflux[1 + i] = zero_plus((R(2) * mu * tiD) * aD);  // 0 + term
+    const R t4 = (R(2) * mu * tiD) * prim[i + 1] * aD;
+    v4 = i == 0 ? zero_plus(t4) : v4 + t4;
     if (i == D) v4 += kc * g[4][D] * aD;
   }
   vflux[4] = v4;

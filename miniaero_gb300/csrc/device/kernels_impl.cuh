@@ -322,8 +322,8 @@ __device__ __forceinline__ void venkat_warp(const TopoView& t, const GeomView<do
       auto evaluate = [&](int q) {
         const double dm = buf.a[q], du = buf.b[q], eps2 = buf.e[q];
         const bool neg = okey(du) < 0;  // du is past the threshold: its sign decides
-        buf.a[q] = negate_if((dm * dm + eps2) * du + 2 * du * du * dm, neg);
-        buf.b[q] = negate_if(du * (dm * dm + 2 * du * du + dm * du + eps2), neg);
+        buf.a[q] = negate_if((dm * dm + eps2) * du + twice(du) * du * dm, neg);
+        buf.b[q] = negate_if(du * (dm * dm + twice(du) * du + dm * du + eps2), neg);
       };
       if (compact) {
         for (unsigned i = lane; i < total; i += 32) evaluate(buf.slot[i]);
@@ -415,7 +415,7 @@ __device__ __forceinline__ void green_gauss_cell(const TopoView& t, const GeomVi
   if (t.axis_cell[c]) {
 #pragma unroll
     for (int p = 0; p < 3; ++p) {
-#pragma unroll (std::is_same<R, float>::value ? 2 : 1)
+#pragma unroll
       for (int q = 0; q < 2; ++q) {
         const int s = 2 * p + q;
         const int code = t.csr_grad[s * C + c];
@@ -431,7 +431,8 @@ __device__ __forceinline__ void green_gauss_cell(const TopoView& t, const GeomVi
           const R pl = left ? wc[k] : wn[k];
           const R pr = left ? wn[k] : wc[k];
           const R gr = halve(pl + pr) * np;
-          acc[k][p] += div(left ? gr : -gr);
+          // acc starts at +0: its first term is 0 + x
+          acc[k][p] = q == 0 ? zero_plus(div(left ? gr : -gr)) : acc[k][p] + div(left ? gr : -gr);
           if (MINMAX) ex[k].face(pl, pr);
         }
       }

@@ -24,7 +24,10 @@ template <class R> __device__ __forceinline__ R dsqrt(R x);
 template <> __device__ __forceinline__ double dsqrt<double>(double x) { return sqrt(x); }
 template <> __device__ __forceinline__ float dsqrt<float>(float x) { return sqrtf(x); }
 template <class R> __device__ __forceinline__ R dabs(R x);
-template <> __device__ __forceinline__ double dabs<double>(double x) { return fabs(x); }
+// |x| as the sign bit cleared on the integer pipe (fabs, for every input).
+template <> __device__ __forceinline__ double dabs<double>(double x) {
+  return __hiloint2double(__double2hiint(x) & 0x7FFFFFFF, __double2loint(x));
+}
 template <> __device__ __forceinline__ float dabs<float>(float x) { return fabsf(x); }
 
 // a / b rounded to nearest, given y = RN(1/b) computed once per divisor.
@@ -60,15 +63,36 @@ __device__ __forceinline__ float div_by_recip(float a, float /*b*/, float y) { r
 // bits in a few instructions.
 //
 // halve(x) = 0.5 * x: for a normal x above the smallest binade the exponent
-// field steps down by one (the product is exact); zeros, subnormals, the
-// smallest binade, infinities and NaNs take the multiply.
+// field steps down by one (the product is exact). Below it (zeros, subnormals,
+// the smallest binade) the pattern is the value in units of 2^-1074, so the
+// result is that integer halved, ties to even; infinities and NaNs return
+// themselves. No FP64 instruction on any path (a multiply in a rarely taken
+// branch would still issue once the compiler predicates the branch).
 __device__ __forceinline__ double halve(double x) {
   const uint32_t hi = static_cast<uint32_t>(__double2hiint(x));
-  if (((hi >> 20) & 0x7FFu) - 2u < 2045u)
-    return __hiloint2double(static_cast<int>(hi - 0x100000u), __double2loint(x));
-  return 0.5 * x;
+  const uint32_t e = (hi >> 20) & 0x7FFu;
+  if (e - 2u < 2045u) return __hiloint2double(static_cast<int>(hi - 0x100000u), __double2loint(x));
+  if (e == 0x7FFu) return x;
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+  const unsigned long long sign = b & 0x8000000000000000ull, m = b ^ sign;
+  return __longlong_as_double(static_cast<long long>(sign | ((m >> 1) + (m & (m >> 1) & 1ull))));
 }
 __device__ __forceinline__ float halve(float x) { return 0.5f * x; }
+// twice(x) = 2 * x: the exponent field steps up by one while the result
+// stays finite (biased exponent 1..2045); from the top binade it overflows to
+// infinity; a zero or subnormal pattern doubles as an integer (exact, and it
+// carries into the exponent field as the value turns normal); infinities and
+// NaNs return themselves. Integer instructions only.
+__device__ __forceinline__ double twice(double x) {
+  const uint32_t hi = static_cast<uint32_t>(__double2hiint(x));
+  const uint32_t e = (hi >> 20) & 0x7FFu;
+  if (e - 1u < 2045u) return __hiloint2double(static_cast<int>(hi + 0x100000u), __double2loint(x));
+  if (e == 0x7FFu) return x;
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+  const unsigned long long sign = b & 0x8000000000000000ull, m = b ^ sign;
+  return __longlong_as_double(static_cast<long long>(sign | (e == 0u ? (m << 1) : 0x7FF0000000000000ull)));
+}
+__device__ __forceinline__ float twice(float x) { return 2.0f * x; }
 // zero_plus(x) = 0 + x in round to nearest: x itself, except that -0 becomes
 // +0 (a sum that starts at +0 and adds x). A NaN stays a NaN.
 __device__ __forceinline__ double zero_plus(double x) {
@@ -77,6 +101,14 @@ __device__ __forceinline__ double zero_plus(double x) {
   return __hiloint2double(negzero ? 0 : static_cast<int>(hi), __double2loint(x));
 }
 __device__ __forceinline__ float zero_plus(float x) { return 0.0f + x; }
+// a < b for an a with a clear sign bit (an absolute value): as signed 64-bit
+// integers the patterns of non-negative doubles keep their order, and a
+// negative b (sign bit set) is below every such a. Same result as the double
+// compare for every b but a NaN.
+__device__ __forceinline__ bool less_nonneg(double a, double b) {
+  return __double_as_longlong(a) < __double_as_longlong(b);
+}
+__device__ __forceinline__ bool less_nonneg(float a, float b) { return a < b; }
 
 // The reciprocal-method quotient without the IEEE fallback, for hot loops
 // that handle the rare cases out of line: `inexact` is set when the quotient
@@ -469,9 +501,9 @@ __device__ __forceinline__ void roe_flux_axis(const R pl[5], const R pr[5], R nD
   const R eig1 = ubar + cbar, eig2 = ubar - cbar, eig3 = ubar;
   R a1 = dabs<R>(eig1), a2 = dabs<R>(eig2), a3 = dabs<R>(eig3);
   const R epuc = efix_u * cfl, epcc = efix_c * cfl;
-  if (a1 < epcc) a1 = R(0.5) * (eig1 * eig1 + epcc * epcc) / epcc;
-  if (a2 < epcc) a2 = R(0.5) * (eig2 * eig2 + epcc * epcc) / epcc;
-  if (a3 < epuc) a3 = R(0.5) * (eig3 * eig3 + epuc * epuc) / epuc;
+  if (less_nonneg(a1, epcc)) a1 = R(0.5) * (eig1 * eig1 + epcc * epcc) / epcc;
+  if (less_nonneg(a2, epcc)) a2 = R(0.5) * (eig2 * eig2 + epcc * epcc) / epcc;
+  if (less_nonneg(a3, epuc)) a3 = R(0.5) * (eig3 * eig3 + epuc * epuc) / epuc;
   const R ep1 = halve(eig1 + a1), em1 = halve(eig1 - a1);
   const R ep2 = halve(eig2 + a2), em2 = halve(eig2 - a2);
   const R ep3 = halve(eig3 + a3), em3 = halve(eig3 - a3);
@@ -626,8 +658,8 @@ __device__ __forceinline__ void viscous_flux_axis(const R g[5][3], const R prim[
   for (int i = 0; i < 3; ++i) {
     const R S = halve(g[i + 1][D] + g[D + 1][i]);
     const R tiD = (i == D) ? S - div3 : S;
-    vflux[1 + i] = zero_plus((R(2) * mu * tiD) * aD);  // 0 + term
-    const R t4 = (R(2) * mu * tiD) * prim[i + 1] * aD;
+    vflux[1 + i] = zero_plus((twice(mu) * tiD) * aD);  // 0 + term
+    const R t4 = (twice(mu) * tiD) * prim[i + 1] * aD;
     v4 = i == 0 ? zero_plus(t4) : v4 + t4;
     if (i == D) v4 += kc * g[4][D] * aD;
   }
@@ -675,8 +707,8 @@ __device__ __forceinline__ bool venkat_ratio(double dumax, double dumin, double 
   const bool pos = kd > okey(1e-40), neg = kd < okey(-1e-40);
   if (!(pos | neg)) return false;
   const double dm = pos ? dumax : dumin;
-  n = negate_if((dm * dm + eps2) * du + 2 * du * du * dm, neg);
-  d = negate_if(du * (dm * dm + 2 * du * du + dm * du + eps2), neg);
+  n = negate_if((dm * dm + eps2) * du + twice(du) * du * dm, neg);
+  d = negate_if(du * (dm * dm + twice(du) * du + dm * du + eps2), neg);
   return true;
 }
 

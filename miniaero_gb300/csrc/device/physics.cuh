@@ -250,20 +250,20 @@ __device__ __forceinline__ void roe_flux(const R pl[5], const R pr[5], const Fac
   const R rl = pl[0], ul = pl[1], vl = pl[2], wl = pl[3];
   const R p_l = rl * R(287.05) * pl[4];
   const R h_l = R(1004.0) * pl[4];
-  const R H_l = h_l + R(0.5) * (ul * ul + vl * vl + wl * wl);
+  const R H_l = h_l + halve(ul * ul + vl * vl + wl * wl);
   const R mf_l = rl * (n[0] * ul + n[1] * vl + n[2] * wl);
   const R rr = pr[0], ur = pr[1], vr = pr[2], wr = pr[3];
   const R p_r = rr * R(287.05) * pr[4];
   const R h_r = R(1004.0) * pr[4];
-  const R H_r = h_r + R(0.5) * (ur * ur + vr * vr + wr * wr);
+  const R H_r = h_r + halve(ur * ur + vr * vr + wr * wr);
   const R mf_r = rr * (n[0] * ur + n[1] * vr + n[2] * wr);
   const R psum = p_l + p_r;
 
-  flux[0] = R(0.5) * (mf_l + mf_r);
-  flux[1] = R(0.5) * (mf_l * ul + mf_r * ur + n[0] * psum);
-  flux[2] = R(0.5) * (mf_l * vl + mf_r * vr + n[1] * psum);
-  flux[3] = R(0.5) * (mf_l * wl + mf_r * wr + n[2] * psum);
-  flux[4] = R(0.5) * (mf_l * H_l + mf_r * H_r);
+  flux[0] = halve(mf_l + mf_r);
+  flux[1] = halve(mf_l * ul + mf_r * ur + n[0] * psum);
+  flux[2] = halve(mf_l * vl + mf_r * vr + n[1] * psum);
+  flux[3] = halve(mf_l * wl + mf_r * wr + n[2] * psum);
+  flux[4] = halve(mf_l * H_l + mf_r * H_r);
 
   const R* nu = f.nu;
   const R* tu = f.tu;
@@ -276,16 +276,16 @@ __device__ __forceinline__ void roe_flux(const R pl[5], const R pr[5], const Fac
   const R vroe = alpha * vl + beta * vr;
   const R wroe = alpha * wl + beta * wr;
   const R hroe = alpha * h_l + beta * h_r +
-                 R(0.5) * alpha * beta *
+                 halve(alpha) * beta *
                      ((ur - ul) * (ur - ul) + (vr - vl) * (vr - vl) + (wr - wl) * (wr - wl));
   const R c = dsqrt<R>(gm1 * hroe);
 
   const R nv = uroe * nu[0] + vroe * nu[1] + wroe * nu[2];
   const R tv = uroe * tu[0] + vroe * tu[1] + wroe * tu[2];
   const R bv = uroe * bu[0] + vroe * bu[1] + wroe * bu[2];
-  const R ke = R(0.5) * (uroe * uroe + vroe * vroe + wroe * wroe);
+  const R ke = halve(uroe * uroe + vroe * vroe + wroe * wroe);
   const R cssi = R(1.0) / (c * c);
-  const R hcssi = R(0.5) * cssi;
+  const R hcssi = halve(cssi);
 
   R dq[5];
   dq[0] = rr - rl;
@@ -300,13 +300,13 @@ __device__ __forceinline__ void roe_flux(const R pl[5], const R pr[5], const Fac
   const R eig1 = ubar + cbar, eig2 = ubar - cbar, eig3 = ubar;
   R a1 = dabs<R>(eig1), a2 = dabs<R>(eig2), a3 = dabs<R>(eig3);
   const R epuc = efix_u * cfl, epcc = efix_c * cfl;
-  if (a1 < epcc) a1 = R(0.5) * (eig1 * eig1 + epcc * epcc) / epcc;
-  if (a2 < epcc) a2 = R(0.5) * (eig2 * eig2 + epcc * epcc) / epcc;
-  if (a3 < epuc) a3 = R(0.5) * (eig3 * eig3 + epuc * epuc) / epuc;
+  if (less_nonneg(a1, epcc)) a1 = R(0.5) * (eig1 * eig1 + epcc * epcc) / epcc;
+  if (less_nonneg(a2, epcc)) a2 = R(0.5) * (eig2 * eig2 + epcc * epcc) / epcc;
+  if (less_nonneg(a3, epuc)) a3 = R(0.5) * (eig3 * eig3 + epuc * epuc) / epuc;
   // |lambda| per characteristic: eigp - eigm of the reference.
-  const R ep1 = R(0.5) * (eig1 + a1), em1 = R(0.5) * (eig1 - a1);
-  const R ep2 = R(0.5) * (eig2 + a2), em2 = R(0.5) * (eig2 - a2);
-  const R ep3 = R(0.5) * (eig3 + a3), em3 = R(0.5) * (eig3 - a3);
+  const R ep1 = halve(eig1 + a1), em1 = halve(eig1 - a1);
+  const R ep2 = halve(eig2 + a2), em2 = halve(eig2 - a2);
+  const R ep3 = halve(eig3 + a3), em3 = halve(eig3 - a3);
   const R lam[5] = {ep1 - em1, ep2 - em2, ep3 - em3, ep3 - em3, ep3 - em3};
 
   // Left eigenvector rows times the conserved jump (MatVec5 with beta = 0).
@@ -320,9 +320,9 @@ __device__ __forceinline__ void roe_flux(const R pl[5], const R pr[5], const Fac
   R ldq[5];
 #pragma unroll
   for (int i = 0; i < 5; ++i) {
-    R acc = R(0.0);
+    R acc = zero_plus(L[i][0] * dq[0]);  // a sum from +0
 #pragma unroll
-    for (int j = 0; j < 5; ++j) acc += L[i][j] * dq[j];
+    for (int j = 1; j < 5; ++j) acc += L[i][j] * dq[j];
     ldq[i] = lam[i] * acc;
   }
   const R hk = hroe + ke;
@@ -334,10 +334,10 @@ __device__ __forceinline__ void roe_flux(const R pl[5], const R pr[5], const Fac
       {(hk + c * nv) * hcssi, (hk - c * nv) * hcssi, (c * c - gm1 * hk) * cssi, tv, bv}};
 #pragma unroll
   for (int i = 0; i < 5; ++i) {
-    R acc = R(0.0);
+    R acc = zero_plus(M[i][0] * ldq[0]);  // a sum from +0
 #pragma unroll
-    for (int j = 0; j < 5; ++j) acc += M[i][j] * ldq[j];
-    flux[i] -= R(0.5) * acc;
+    for (int j = 1; j < 5; ++j) acc += M[i][j] * ldq[j];
+    flux[i] -= halve(acc);
   }
 }
 
@@ -743,14 +743,14 @@ __device__ __forceinline__ R vanalbada(R dumax, R dumin, R du) {
 // sqrt(((0 + n0^2) + n1^2) + n2^2), which equals the Roe |n|.
 template <class R>
 __device__ __forceinline__ void reflect_state(const R n[3], R nn, const R pl[5], R pr[5]) {
-  R ub = R(0.0);
-  ub += pl[1] * n[0] / nn;
+  R ub = zero_plus(pl[1] * n[0] / nn);  // a sum from +0
   ub += pl[2] * n[1] / nn;
   ub += pl[3] * n[2] / nn;
+  const R ub2 = twice(ub);
   pr[0] = pl[0];
-  pr[1] = pl[1] - R(2) * ub * n[0] / nn;
-  pr[2] = pl[2] - R(2) * ub * n[1] / nn;
-  pr[3] = pl[3] - R(2) * ub * n[2] / nn;
+  pr[1] = pl[1] - ub2 * n[0] / nn;
+  pr[2] = pl[2] - ub2 * n[1] / nn;
+  pr[3] = pl[3] - ub2 * n[2] / nn;
   pr[4] = pl[4];
 }
 

@@ -395,8 +395,10 @@ ma_status ma_debug_binsort(const int32_t* keys, int32_t n, int32_t* perm);
  * all-ones significand, 2 quotients near rounding midpoints); mode 3 checks
  * the integer float->double widening of the mixed form instead, mode 4 its
  * integer double->float rounding; mode 5 divides tiny, subnormal and zero
- * numerators. Returns the mismatch count and, if any, one failing pair in
- * example[0..1]. */
+ * numerators; mode 6 checks the FP64 identities the plain form evaluates with
+ * integer instructions (0.5*x, 2*x, 0+x, |x|, and x < y for a non-negative x)
+ * against the FP64 instructions, over every exponent class. Returns the
+ * mismatch count and, if any, one failing pair in example[0..1]. */
 ma_status ma_debug_check_division(int32_t mode, uint64_t n, uint64_t seed, uint64_t* mismatches, double* example);
 
 /* Measured FP64 issue rate of this device (thread instructions per second):

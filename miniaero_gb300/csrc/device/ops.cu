@@ -131,7 +131,8 @@ __device__ __forceinline__ double make_double(uint64_t r, int e0, int span, bool
 // div_by_recip against the IEEE quotient on generated operand pairs.
 // mode 0: random a and b; 1: b with an all-ones significand (possibly a few
 // bits cleared); 2: quotients close to a rounding midpoint; 5: tiny,
-// subnormal and zero numerators (3 and 4 check the float conversions).
+// subnormal and zero numerators (3 and 4 check the float conversions, 6 the
+// FP64 identities done with integer instructions).
 __global__ void k_check_division(int mode, unsigned long long n, unsigned long long seed,
                                  unsigned long long* mismatches, double* example) {
   const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
@@ -182,6 +183,33 @@ __global__ void k_check_division(int mode, unsigned long long n, unsigned long l
       if (!same && atomicAdd(mismatches, 1ull) == 0ull) {
         example[0] = static_cast<double>(f);
         example[1] = w;
+      }
+      continue;
+    }
+    if (mode == 6) {
+      // The FP64 identities taken on the integer pipe against the FP64
+      // instructions they replace: halve = 0.5 * x, twice = 2 * x,
+      // zero_plus = 0 + x, dabs = fabs and less_nonneg(|x|, y) = |x| < y (y not
+      // a NaN), over every exponent class (zeros, subnormals, the smallest and
+      // largest binades, infinities and NaNs, and random normal values).
+      uint64_t bits = r1;
+      const uint32_t kind = static_cast<uint32_t>(r3 & 7u);
+      const uint64_t E = kind == 0u ? 0u : kind == 1u ? 1u : kind == 2u ? 2u : kind == 3u ? 2045u
+                       : kind == 4u ? 2046u : kind == 5u ? 2047u : ((r2 >> 52) & 0x7FFu);
+      bits = (bits & 0x800FFFFFFFFFFFFFull) | (E << 52);
+      if (((r3 >> 3) & 15u) == 0u) bits &= 0x8000000000000000ull | (E << 52);  // zero significand
+      const double x = __longlong_as_double(static_cast<long long>(bits));
+      const double y = __longlong_as_double(static_cast<long long>(r2));
+      auto same = [](double p, double q) {
+        return (q != q) ? (p != p) : (__double_as_longlong(p) == __double_as_longlong(q));
+      };
+      const double ax = fabs(x);
+      bool ok = same(halve(x), __dmul_rn(0.5, x)) && same(twice(x), __dmul_rn(2.0, x)) &&
+                same(zero_plus(x), __dadd_rn(0.0, x)) && same(dabs<double>(x), ax);
+      if (y == y && x == x) ok = ok && (less_nonneg(ax, y) == (ax < y)) && (less_nonneg(ax, x) == (ax < x));
+      if (!ok && atomicAdd(mismatches, 1ull) == 0ull) {
+        example[0] = x;
+        example[1] = y;
       }
       continue;
     }

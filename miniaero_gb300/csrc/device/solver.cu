@@ -971,7 +971,7 @@ extern "C" ma_status ma_op_limiter(int32_t n, int32_t kind, const double* dumax,
 
 extern "C" ma_status ma_debug_check_division(int32_t mode, uint64_t n, uint64_t seed, uint64_t* mismatches,
                                              double* example) {
-  if (!mismatches || !example || mode < 0 || mode > 5) return set_error(MA_EINVAL, "ma_debug_check_division: bad arguments");
+  if (!mismatches || !example || mode < 0 || mode > 6) return set_error(MA_EINVAL, "ma_debug_check_division: bad arguments");
   DevBufs b;
   double* dex;
   MA_CUDA_TRY(b.in(nullptr, 3, &dex));

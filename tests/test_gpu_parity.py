@@ -234,7 +234,7 @@ def test_mixed_flat_plate_density_error(has_gpu):
 
 
 # ---- exact division used by the gradient ------------------------------------------------
-@pytest.mark.parametrize("mode", [0, 1, 2, 3, 4, 5])
+@pytest.mark.parametrize("mode", [0, 1, 2, 3, 4, 5, 6])
 def test_reciprocal_division_is_correctly_rounded(has_gpu, mode):
     """div_by_recip(a, b, RN(1/b)) equals the IEEE quotient a/b bit for bit
     (2^28 pairs per mode; mode 5: numerators from the subnormal range to
@@ -242,7 +242,9 @@ def test_reciprocal_division_is_correctly_rounded(has_gpu, mode):
     IEEE division); mode 3: widen_exact equals the float->double conversion
     on 2^28 random bit patterns (subnormals: signed zero); mode 4: narrow_rn
     equals the double->float conversion (random patterns, both edges of the
-    float range, exact midpoints and their neighbours)."""
+    float range, exact midpoints and their neighbours); mode 6: the integer
+    forms of 0.5*x, 2*x, 0+x, |x| and x < y (x >= 0) equal the FP64
+    instructions on 2^28 patterns of every exponent class."""
     import ctypes
     from miniaero_gb300 import _lib
     mism = ctypes.c_uint64(0)

@@ -503,6 +503,7 @@ __device__ __forceinline__ void sweep1_cell(const TopoView& t, const GeomView<R>
   for (int k = 0; k < 5; ++k) wc[k] = W[k * C + c];
   const R V = g.vol[c];
   const R Vinv = g.vinv[c];  // RN(1/V), see div_by_recip
+  const R Vlo = recip_lo(V, Vinv);  // 1/V = Vinv + Vlo for the 30 divisions below
   R acc[5][3];
   Extrema<R> ex[5];
 #pragma unroll
@@ -512,7 +513,7 @@ __device__ __forceinline__ void sweep1_cell(const TopoView& t, const GeomView<R>
   const int ac = t.axis_cell[c];
   bool inexact = false;  // some term's reciprocal quotient may differ from the IEEE one
   green_gauss_cell<R, (MODE > 0)>(t, g, W, c, wc, acc, ex,
-                                  [&](R a) { return div_by_recip_flag(a, V, Vinv, inexact); });
+                                  [&](R a) { return div_by_recip2_flag(a, V, Vinv, Vlo, inexact); });
   R gsum[5][3];
   bool exact_done = false;
   if constexpr (std::is_same<R, double>::value) {

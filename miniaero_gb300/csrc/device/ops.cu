@@ -223,7 +223,12 @@ __global__ void k_check_division(int mode, unsigned long long n, unsigned long l
     const double y = 1.0 / b;
     const double q = div_by_recip(a, b, y);
     const double ref = a / b;
-    if (__double_as_longlong(q) != __double_as_longlong(ref)) {  // zeros included, with their sign
+    // The sweep's form with the two-part reciprocal, where it does not flag
+    // the quotient for the IEEE division (zero quotients of either sign).
+    bool inexact = false;
+    const double q2 = div_by_recip2_flag(a, b, y, recip_lo(b, y), inexact);
+    const bool ok2 = inexact || (a == 0.0 ? q2 == 0.0 : __double_as_longlong(q2) == __double_as_longlong(ref));
+    if (__double_as_longlong(q) != __double_as_longlong(ref) || !ok2) {  // zeros included, with their sign
       if (atomicAdd(mismatches, 1ull) == 0ull) {
         example[0] = a;
         example[1] = b;

@@ -110,24 +110,34 @@ __device__ __forceinline__ bool less_nonneg(double a, double b) {
 }
 __device__ __forceinline__ bool less_nonneg(float a, float b) { return a < b; }
 
-// The reciprocal-method quotient without the IEEE fallback, for hot loops
-// that handle the rare cases out of line: `inexact` is set when the quotient
-// may differ from a/b (the conditions of div_by_recip, with zero numerators
-// excluded: their quotient is a zero of either sign, and the callers only
-// add it to sums that start at +0, where the sign of a zero never shows).
-__device__ __forceinline__ double div_by_recip_flag(double a, double b, double y, bool& inexact) {
-  double q = a * y;
+
+// Low-order part of the reciprocal: for y = RN(1/b) the residual 1 - b*y is
+// exact (one FMA), and y + ylo with ylo = RN((1 - b*y) * y) is 1/b to about
+// 2^-105 relative. For callers that divide many values by one b.
+__device__ __forceinline__ double recip_lo(double b, double y) { return fma(-b, y, 1.0) * y; }
+__device__ __forceinline__ float recip_lo(float /*b*/, float /*y*/) { return 0.0f; }
+
+// a / b for hot loops that divide many values by one b, with the IEEE
+// fallback left to the caller. With the two-part reciprocal y + ylo,
+// q1 = RN(a*y + RN(a*ylo)) is within 2^-104 relative of a/b before its
+// rounding, hence faithful, so Markstein's correction RN(q1 + (a - b*q1)*y)
+// alone gives the correctly rounded quotient: one multiply and three FMAs
+// (div_by_recip takes one and four). `inexact` is set under div_by_recip's
+// range conditions, where the result may differ from a/b; zero numerators
+// are excluded: their quotient is a zero of either sign, and the callers only
+// add it to sums that start at +0, where the sign of a zero never shows.
+__device__ __forceinline__ double div_by_recip2_flag(double a, double b, double y, double ylo, bool& inexact) {
+  const double q = fma(a, y, a * ylo);
   const uint32_t eq = (static_cast<uint32_t>(__double2hiint(q)) >> 20) & 0x7FFu;
   const uint32_t eb = (static_cast<uint32_t>(__double2hiint(b)) >> 20) & 0x7FFu;
   const uint32_t ah = static_cast<uint32_t>(__double2hiint(a)) & 0x7FFFFFFFu;
   const bool range = (eq + eb < 1086u) | (eq == 0x7FFu) | (eb - 1u > 2043u);
   inexact |= range & ((ah | static_cast<uint32_t>(__double2loint(a))) != 0u);
-  double r = fma(-q, b, a);
-  q = fma(r, y, q);
-  r = fma(-q, b, a);
-  return fma(r, y, q);
+  return fma(fma(-q, b, a), y, q);
 }
-__device__ __forceinline__ float div_by_recip_flag(float a, float /*b*/, float y, bool& /*inexact*/) { return a * y; }
+__device__ __forceinline__ float div_by_recip2_flag(float a, float /*b*/, float y, float /*ylo*/, bool& /*inexact*/) {
+  return a * y;
+}
 
 // float -> double by bit manipulation on the integer pipe (the FP64 pipe is
 // the residual kernel's bottleneck): exact for normal floats, zeros, inf and

@@ -804,14 +804,17 @@ __device__ __forceinline__ void residual_cell(const TopoView& t, const R* __rest
     // reference does; the mixed form (FP64 update, no reference bits to keep)
     // fuses them, an explicit fma that gives the same bits in every build.
     auto axpy = [&](double x, double a) { return kPlain ? x + a * r : fma(a, r, x); };
+    // The plain form's alpha_next * r for stages 0-2: 0.5 r and 1 r, exact
+    // without the FP64 multiply (the mixed form folds dt/V into ca instead).
+    auto next = [&](double x) { return kPlain ? x + (stage == 2 ? r : halve(r)) : fma(ca, r, x); };
     if (stage == 0) {
       const double un = Un[k * C + c];
       Unp1[k * C + c] = axpy(un, cb);
-      ut[k] = axpy(un, ca);
+      ut[k] = next(un);
     } else if (stage < 3) {
       const double un = Un[k * C + c];
       Unp1[k * C + c] = axpy(Unp1[k * C + c], cb);
-      ut[k] = axpy(un, ca);
+      ut[k] = next(un);
     } else {
       const double u1 = axpy(Unp1[k * C + c], cb);
       Un[k * C + c] = u1;

@@ -235,7 +235,7 @@ __device__ __forceinline__ void primitives(const double U[5], double V[5]) {
   const double u = U[1] * ri;
   const double v = U[2] * ri;
   const double w = U[3] * ri;
-  const double k = 0.5 * (u * u + v * v + w * w);
+  const double k = halve(u * u + v * v + w * w);
   const double e = U[4] * ri - k;
   const double T = div_by_recip(e * (gamma - 1.0), Rgas, kRgasInv);
   V[0] = r; V[1] = u; V[2] = v; V[3] = w; V[4] = T;
@@ -529,7 +529,8 @@ __device__ __forceinline__ void roe_flux_axis(const R pl[5], const R pr[5], R nD
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
     row0[1 + j] = (j == D) ? c * nuD - gm1 * vroe[j] : -(gm1 * vroe[j]);
-    row1[1 + j] = (j == D) ? -c * nuD - gm1 * vroe[j] : -(gm1 * vroe[j]);
+    // (-c) nu_D is -(c nu_D) exactly (round to nearest is symmetric): one product for both rows.
+    row1[1 + j] = (j == D) ? -(c * nuD) - gm1 * vroe[j] : -(gm1 * vroe[j]);
   }
   row0[4] = gm1;
   row1[4] = gm1;
@@ -575,7 +576,7 @@ __device__ __forceinline__ void roe_flux_axis(const R pl[5], const R pr[5], R nD
       acc = zero_plus(vroe[j] * hcssi * ldq[0]);
       acc += vroe[j] * hcssi * ldq[1];
     }
-    acc += -gm1 * vroe[j] * cssi * ldq[2];
+    acc += -(gm1 * vroe[j]) * cssi * ldq[2];  // (-gm1) u_j, as the rows' product negated
     if (j == T) acc += tuT * ldq[3];
     if (j == B) acc += buB * ldq[4];
     flux[1 + j] -= halve(acc);

@@ -110,7 +110,6 @@ __device__ __forceinline__ bool less_nonneg(double a, double b) {
 }
 __device__ __forceinline__ bool less_nonneg(float a, float b) { return a < b; }
 
-
 // Low-order part of the reciprocal: for y = RN(1/b) the residual 1 - b*y is
 // exact (one FMA), and y + ylo with ylo = RN((1 - b*y) * y) is 1/b to about
 // 2^-105 relative. For callers that divide many values by one b.

@@ -566,7 +566,9 @@ def run_ours(args, world, rank, local):
             results[name]["one_launch"] = one_launch_value(ma, name, timed, args.warmup)
 
     batched = serving = None
-    if not args.no_extras:
+    # The batch and serving sections describe one GPU: with replicas (N > 1)
+    # they would hold every GPU for minutes to report rank 0's copy again.
+    if not args.no_extras and world == 1:
         batched = run_batched(ma, steps=max(2, min(args.steps, 10)), warmup=args.warmup)
         serving = run_serving_suite(ma, n_requests=args.serve_requests)
 

@@ -28,6 +28,7 @@ namespace {
 
 constexpr int kCellBlock = 256;
 constexpr int kFaceBlock = 128;
+constexpr int kSmallMeshCells = 152 * kCellBlock * 2;
 // Resident sweep blocks per SM: the FP32 sweep waits on dependent gathers; at
 // 4 blocks (64 registers, no spill) it runs 12 % faster than at 5 (48
 // registers, 44 bytes spilled) with the approximate FP32 division. The FP64
@@ -1142,8 +1143,13 @@ cudaError_t launch_stage_impl(const TopoView& t, const GeomView<R>& g, const Pat
     for (int k = 0; k < 5; ++k) inflow.u[k] = cfg.inflow[k];
     k_bc_flux<R><<<blocks_for(t.Fb, kFaceBlock), kFaceBlock, 0, stream>>>(t, g, b.W, cfg.transport, inflow, b.fflux);
   }
-  if (kernels & kResidual)
-    k_residual<R><<<gc, kCellBlock, 0, stream>>>(t, b.fflux, s.Un, s.Unp1, b.W, s.res, cfg.dt, stage, cfg.cell_flux);
+  if (kernels & kResidual) {
+    // Meshes of up to two blocks of 256 cells per SM (152 SMs): 32-cell blocks
+    // spread the cells over every SM; 256-cell blocks would leave SMs idle.
+    const int rb = t.C <= kSmallMeshCells ? 32 : kCellBlock;
+    k_residual<R><<<blocks_for(t.C, rb), rb, 0, stream>>>(t, b.fflux, s.Un, s.Unp1, b.W, s.res, cfg.dt, stage,
+                                                         cfg.cell_flux);
+  }
   return cudaGetLastError();
 }
 

@@ -309,9 +309,9 @@ __device__ __forceinline__ void roe_flux(const R pl[5], const R pr[5], const Fac
   const R eig1 = ubar + cbar, eig2 = ubar - cbar, eig3 = ubar;
   R a1 = dabs<R>(eig1), a2 = dabs<R>(eig2), a3 = dabs<R>(eig3);
   const R epuc = efix_u * cfl, epcc = efix_c * cfl;
-  if (less_nonneg(a1, epcc)) a1 = R(0.5) * (eig1 * eig1 + epcc * epcc) / epcc;
-  if (less_nonneg(a2, epcc)) a2 = R(0.5) * (eig2 * eig2 + epcc * epcc) / epcc;
-  if (less_nonneg(a3, epuc)) a3 = R(0.5) * (eig3 * eig3 + epuc * epuc) / epuc;
+  if (less_nonneg(a1, epcc)) a1 = halve(eig1 * eig1 + epcc * epcc) / epcc;
+  if (less_nonneg(a2, epcc)) a2 = halve(eig2 * eig2 + epcc * epcc) / epcc;
+  if (less_nonneg(a3, epuc)) a3 = halve(eig3 * eig3 + epuc * epuc) / epuc;
   // |lambda| per characteristic: eigp - eigm of the reference.
   const R ep1 = halve(eig1 + a1), em1 = halve(eig1 - a1);
   const R ep2 = halve(eig2 + a2), em2 = halve(eig2 - a2);
@@ -510,9 +510,9 @@ __device__ __forceinline__ void roe_flux_axis(const R pl[5], const R pr[5], R nD
   const R eig1 = ubar + cbar, eig2 = ubar - cbar, eig3 = ubar;
   R a1 = dabs<R>(eig1), a2 = dabs<R>(eig2), a3 = dabs<R>(eig3);
   const R epuc = efix_u * cfl, epcc = efix_c * cfl;
-  if (less_nonneg(a1, epcc)) a1 = R(0.5) * (eig1 * eig1 + epcc * epcc) / epcc;
-  if (less_nonneg(a2, epcc)) a2 = R(0.5) * (eig2 * eig2 + epcc * epcc) / epcc;
-  if (less_nonneg(a3, epuc)) a3 = R(0.5) * (eig3 * eig3 + epuc * epuc) / epuc;
+  if (less_nonneg(a1, epcc)) a1 = halve(eig1 * eig1 + epcc * epcc) / epcc;
+  if (less_nonneg(a2, epcc)) a2 = halve(eig2 * eig2 + epcc * epcc) / epcc;
+  if (less_nonneg(a3, epuc)) a3 = halve(eig3 * eig3 + epuc * epuc) / epuc;
   const R ep1 = halve(eig1 + a1), em1 = halve(eig1 - a1);
   const R ep2 = halve(eig2 + a2), em2 = halve(eig2 - a2);
   const R ep3 = halve(eig3 + a3), em3 = halve(eig3 - a3);
